@@ -1,0 +1,195 @@
+/*
+ * heal_gb300.h — C ABI of the GB300 HEAL vendor backend.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and tensor
+ * descriptors, and returns an `int` status (0 = success).  On failure the
+ * message is available from heal_last_error() and the status names the C++
+ * exception type the HEAL API throws for it (HEAL_ERR_INVALID_ARGUMENT ->
+ * std::invalid_argument, ...).  No torch or CUDA types appear here.
+ *
+ * Each function cites the HEAL interface it replaces as
+ * `path:line` inside the Lattica-ai/heal project.  The C++ templates of
+ * `namespace lattica_hw_api` (the include/ headers of HEAL) and the `lattica_hw`
+ * Python module are thin layers over these calls.
+ *
+ * Execution model: one GPU, one library stream (replaceable with
+ * heal_set_stream).  Compute calls are stream-ordered and return once the
+ * work is enqueued; results are visible to every later call on the same
+ * stream, and heal_d2h / heal_synchronize wait for them.  A call validates
+ * its arguments on the host before it enqueues anything, so argument errors
+ * leave every output untouched.  Tables that depend on data (a permutation's
+ * range, a modulus' constants, a twiddle table's Shoup companions) are
+ * derived on the GPU the first time a table is used and cached per
+ * allocation; the first use of a permutation table synchronises once so that
+ * an out-of-range index is reported by the call that uses it.
+ */
+#ifndef HEAL_GB300_H
+#define HEAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HEAL_MAX_DIMS 8
+
+/* Element types of DeviceTensor<T>: T = int32_t, int64_t, double. */
+typedef enum heal_dtype {
+  HEAL_INT32 = 0,
+  HEAL_INT64 = 1,
+  HEAL_FLOAT64 = 2
+} heal_dtype;
+
+/* Status codes; each maps to the exception HEAL's C++ API throws. */
+typedef enum heal_status {
+  HEAL_OK = 0,
+  HEAL_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument */
+  HEAL_ERR_OUT_OF_RANGE = 2,     /* std::out_of_range     */
+  HEAL_ERR_RUNTIME = 3,          /* std::runtime_error    */
+  HEAL_ERR_BAD_ALLOC = 4,        /* std::bad_alloc        */
+  HEAL_ERR_CUDA = 5              /* CUDA failure (std::runtime_error) */
+} heal_status;
+
+/*
+ * A strided view of device memory: the fields of HEAL's DeviceTensor<T>
+ * (example_impl/device_memory_impl.h:11-34 — dims, strides, data).
+ * `data` is the device address of element (0, ..., 0); strides are in
+ * elements and may be 0 (a broadcast axis made by expand/unsqueeze).
+ */
+typedef struct heal_tensor {
+  void *data;
+  int32_t dtype; /* heal_dtype */
+  int32_t ndim;  /* 0 .. HEAL_MAX_DIMS */
+  int64_t dims[HEAL_MAX_DIMS];
+  int64_t strides[HEAL_MAX_DIMS];
+} heal_tensor;
+
+/* ---------------------------------------------------------------- runtime */
+
+/* Selects the CUDA device and creates the library stream and memory pool.
+ * Called implicitly by every other entry point with the current device. */
+int heal_init(int device);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *heal_last_error(void);
+
+/* Waits for all enqueued work, then prints (to stderr) the diagnostics
+ * kernels recorded since the last synchronisation, e.g. the
+ * g_decomposition capacity warnings (g_decomposition_impl.cpp:58-65). */
+int heal_synchronize(void);
+
+/* The stream every compute call is enqueued on (a cudaStream_t). */
+void *heal_get_stream(void);
+/* Replaces the library stream by a caller's cudaStream_t (NULL restores the
+ * library's own stream). */
+int heal_set_stream(void *stream);
+
+/* Number of kernels this library has launched since heal_init. */
+uint64_t heal_kernel_launch_count(void);
+
+/* ------------------------------------------- device memory (HBM residency)
+ * Replaces allocate_on_hardware / host_to_device / device_to_host
+ * (include/device_memory.h:24-39; example_impl/device_memory_impl.cpp:168-202). */
+
+/* Allocates `bytes` of HBM (stream-ordered pool).  `zero` != 0 clears it,
+ * as allocate_on_hardware's calloc does (device_memory_impl.cpp:171). */
+int heal_alloc(size_t bytes, int zero, void **out);
+/* Releases memory from heal_alloc (stream-ordered). */
+int heal_free(void *ptr);
+/* Host -> device copy of `bytes` (pageable or pinned host memory).
+ * Enqueued on the library stream; returns when the source may be reused. */
+int heal_h2d(void *dst_device, const void *src_host, size_t bytes);
+/* Device -> host copy; waits for all earlier work on the stream first. */
+int heal_d2h(void *dst_host, const void *src_device, size_t bytes);
+/* Asynchronous variants for pinned host memory (no wait). */
+int heal_h2d_async(void *dst_device, const void *src_host, size_t bytes);
+int heal_d2h_async(void *dst_host, const void *src_device, size_t bytes);
+/* Pinned host memory for the async copies. */
+int heal_host_alloc(size_t bytes, void **out);
+int heal_host_free(void *ptr);
+/* Declares that memory from heal_alloc was written by something other than
+ * this library, so tables derived from it are rebuilt on their next use. */
+int heal_mark_modified(void *ptr);
+
+/* Strided gather of `src` into `dst` (same dims, any strides, any dtype):
+ * the copy inside make_contiguous (include/contiguous.h:19-20;
+ * example_impl/contiguous_impl.cpp:9-52). */
+int heal_copy_strided(const heal_tensor *src, const heal_tensor *dst);
+
+/* ------------------------------------ stride-only metadata (no GPU access)
+ * In-place edits of a descriptor, as DeviceTensor::reshape
+ * (device_memory_impl.cpp:42-84) and expand / squeeze / unsqueeze
+ * (include/memory_virtual_ops.h:39-86; memory_virtual_ops_impl.cpp:7-86). */
+int heal_tensor_reshape(heal_tensor *t, int32_t new_ndim, const int64_t *new_dims);
+int heal_tensor_expand(heal_tensor *t, int64_t axis, int64_t repeats);
+int heal_tensor_squeeze(heal_tensor *t, int64_t axis);
+int heal_tensor_unsqueeze(heal_tensor *t, int64_t axis);
+/* Extension (no HEAL counterpart; named by DeviceDispatcher.moveaxis,
+ * python_execution/lattica_heal_runtime/device_interface.py:84-85):
+ * moves axis `src` to position `dst` by permuting dims and strides. */
+int heal_tensor_moveaxis(heal_tensor *t, int64_t src, int64_t dst);
+/* Extension: basic slice [start, stop) with positive step along `axis`. */
+int heal_tensor_slice(heal_tensor *t, int64_t axis, int64_t start, int64_t stop, int64_t step);
+/* 1 if dense row-major ignoring size-1 axes (device_memory_impl.cpp:31-40). */
+int heal_tensor_is_contiguous(const heal_tensor *t);
+/* Elements spanned by the view: 1 + sum((dims[i]-1)*strides[i])
+ * (device_memory_impl.cpp:19-23); 0 if any dim is 0. */
+int64_t heal_tensor_span(const heal_tensor *t);
+
+/* ------------------------------------------- modular elementwise arithmetic
+ * result = (a op b) % p in the double-width type (int32 -> int64,
+ * int64 -> __int128) with C's truncating remainder, broadcasting a, b and p
+ * against result's shape (include/modop.h:47-111;
+ * example_impl/modop_impl.cpp:108-180,238-239).  Scalars are given as
+ * int64_t and converted to the element type, as the templates' T scalars. */
+int heal_modmul_ttt(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *result);
+int heal_modmul_ttc(const heal_tensor *a, const heal_tensor *b, int64_t p, const heal_tensor *result);
+int heal_modmul_tct(const heal_tensor *a, int64_t b, const heal_tensor *p, const heal_tensor *result);
+int heal_modmul_tcc(const heal_tensor *a, int64_t b, int64_t p, const heal_tensor *result);
+int heal_modsum_ttt(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *result);
+int heal_modsum_ttc(const heal_tensor *a, const heal_tensor *b, int64_t p, const heal_tensor *result);
+int heal_modsum_tct(const heal_tensor *a, int64_t b, const heal_tensor *p, const heal_tensor *result);
+int heal_modsum_tcc(const heal_tensor *a, int64_t b, int64_t p, const heal_tensor *result);
+
+/* result = a % b with C's remainder in the element type, identical shapes
+ * (include/modop.h:115-134; modop_impl.cpp:188-235). */
+int heal_mod_tt(const heal_tensor *a, const heal_tensor *b, const heal_tensor *result);
+int heal_mod_tc(const heal_tensor *a, int64_t b, const heal_tensor *result);
+int heal_mod_ct(int64_t a, const heal_tensor *b, const heal_tensor *result);
+
+/* Extension (DeviceDispatcher._modneg_tt / _modneg_tc,
+ * device_interface.py:51-54, which have no backend in HEAL):
+ * result = (p - a % p) % p in the double-width type, broadcasting like
+ * modsum. */
+int heal_modneg_tt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *result);
+int heal_modneg_tc(const heal_tensor *a, int64_t p, const heal_tensor *result);
+
+/* Reduction of a non-last axis modulo p[k] (include/axis_modsum.h:24-30;
+ * example_impl/axis_modsum_impl.cpp:12-76). */
+int heal_axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_tensor *result, int64_t axis);
+
+/* Base-2^base_bits digits of every element into a new last axis of size
+ * `power` (include/g_decomposition.h:24-30; g_decomposition_impl.cpp:10-67). */
+int heal_g_decomposition(const heal_tensor *a, const heal_tensor *result, uint64_t power, uint64_t base_bits);
+
+/* Batched negacyclic NTT / INTT over [l, m, r, k] with moduli innermost
+ * (include/ntt.h:31-52; example_impl/ntt_impl.cpp:69-170).  log2p and mu
+ * may be NULL (HEAL declares them optional and its sample ignores them).
+ * The inverse scales by m_inv in the double-width type. */
+int heal_ntt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm, const heal_tensor *twiddles,
+             const heal_tensor *log2p, const heal_tensor *mu, const heal_tensor *result);
+int heal_intt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm, const heal_tensor *inv_twiddles,
+              const heal_tensor *m_inv, const heal_tensor *log2p, const heal_tensor *mu, const heal_tensor *result);
+
+/* Per-row gather along perm_axis with indices perms[l, m]
+ * (include/permute.h:33-40; example_impl/permute_impl.cpp:8-65). */
+int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tensor *result, int64_t elementwise_axis,
+                 int64_t perm_axis);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* HEAL_GB300_H */
