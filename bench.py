@@ -1,0 +1,319 @@
+"""Benchmark of the HEAL hot path on one GB300: the keyswitch-shaped chain.
+
+Workload (one step): a ciphertext ct[2][L=24][N=2^16] of int64 residues
+under the 24 largest 50-bit primes q = 1 (mod 2N), through INTT,
+g_decomposition (D = 3 digits of base 2^17), NTT of the 72 digit limbs,
+modmul against a key[3][2][24][2^16], axis_modsum over the digits, and the
+Galois permutation X -> X^5.  Each HEAL call is one C-ABI call.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Printed: one JSON line (rank 0).  `value` is chains/s with inputs resident
+in HBM, timed with CUDA events on the library stream; inputs rotate through
+8 ciphertexts (192 MiB) and 8 outputs, more than the 126 MiB L2, so no step
+reads the previous step's data from L2.  `e2e` is the same through the C ABI
+from pinned host buffers (H2D of ct and D2H of the result inside the timed
+region).  `roofline` covers the batched NTT of the digits.  `cpu_baseline`
+times the CPU oracle (a restatement of HEAL's example_impl) on this host.
+
+--impl reference times the CPU oracle itself on all host cores, four limbs of
+the chain per step (every limb is independent), scaled to chains/s.
+Under torchrun with N > 1 every rank runs its own chains on its own GPU
+(replicas, no collective on the data path); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, L, D, BITS, BOUND = 1 << 16, 24, 3, 17, 50
+METRIC = "batched NTT limbs/s & keyswitch chains/s on 1 GB300, bit-exact, % HBM roofline"
+CONFIG = {"workload": "keyswitch chain: ct[2][24][65536] int64, 50-bit NTT primes, INTT -> g_decomposition "
+                      "(D=3, base 2^17) -> NTT(72 limbs) -> modmul(key[3][2][24][65536]) -> axis_modsum(digits) "
+                      "-> permute(X->X^5)",
+          "N": N, "limbs": L, "digits": D, "base_bits": BITS, "prime_bits": BOUND,
+          "l2": "inputs rotate through 8 ciphertexts (192 MiB) and 8 outputs, larger than L2",
+          "parallelism": "replicas per GPU (limb/ciphertext sharding needs no collective)"}
+RING = 8
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per NTT call from the committed ncu summary, if present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ntt_traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------------- CPU
+SAMPLE_LIMBS = 4   # limbs per CPU run: 24 NTT columns, enough to keep every core busy
+
+
+def sample_limbs(run):
+    return [(run * SAMPLE_LIMBS + i) % L for i in range(SAMPLE_LIMBS)]
+
+
+def cpu_sample(ch_host, ct, seconds=10.0):
+    """Oracle chain restricted to SAMPLE_LIMBS limbs per run, repeated for
+    ~`seconds`; returns (chains/s, threads, runs)."""
+    from heal_gb300.chain import oracle_chain
+    from oracle import oracle as O
+    threads = O.set_threads(os.cpu_count() or 1)
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        oracle_chain(ch_host, ct, D, BITS, limb_idx=sample_limbs(runs))
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return runs * SAMPLE_LIMBS / el / L, threads, runs
+
+
+def reference_arm(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    from heal_gb300 import params as P
+    from heal_gb300.chain import oracle_chain
+    from oracle import build as ob
+    from oracle import oracle as O
+    ob.build()
+    qs = P.ntt_primes(1 << BOUND, N, L)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, N)
+    host = {"p": p, "perm": perm, "tw": tw, "itw": itw, "minv": minv,
+            "key": P.residues(7, (2, N, 1, L * D), np.repeat(p, D)),
+            "gal": P.galois_perm(N, 5).reshape(1, N)}
+    ct = P.residues(1000, (2, N, 1, L), qs)
+    threads = O.set_threads(os.cpu_count() or 1)
+    for w in range(args.warmup):
+        oracle_chain(host, ct, D, BITS, limb_idx=sample_limbs(w))
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        oracle_chain(host, ct, D, BITS, limb_idx=sample_limbs(s))
+    el = time.perf_counter() - t0
+    value = args.steps * SAMPLE_LIMBS / el / L
+    sample = (f"{SAMPLE_LIMBS} of the 24 limbs per step (chain output limbs are independent), "
+              f"{args.steps} steps, scaled by {SAMPLE_LIMBS}/24")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "chains/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic", "config": CONFIG,
+            "cpu_baseline": {"value": value, "unit": "chains/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "chains/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------- GPU
+def our_arm(args):
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import heal_gb300
+    from heal_gb300 import capi
+    from heal_gb300 import params as P
+    from heal_gb300.chain import KeyswitchChain
+    heal_gb300.build()
+    capi.check(capi.lib().heal_init(local))
+    stream = torch.cuda.ExternalStream(capi.stream())
+
+    ch = KeyswitchChain(n=N, limbs=L, digits=D, base_bits=BITS, bound_bits=BOUND)
+    cts_host = [P.residues(1000 + i, ch.shape(), ch.qs) for i in range(RING)]
+    cts = [capi.DeviceArray.from_numpy(c) for c in cts_host]
+    outs = [capi.DeviceArray.empty(ch.shape(), np.int64) for _ in range(RING)]
+
+    def barrier():
+        torch.cuda.synchronize()
+        capi.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(fn, steps):
+        barrier()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = capi.launches()
+        start.record(stream)
+        for s in range(steps):
+            fn(s)
+        stop.record(stream)
+        stop.synchronize()
+        barrier()
+        ms = start.elapsed_time(stop)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, capi.launches() - l0
+
+    # ---- correctness of the timed configuration (one step, spot-checked)
+    ch.run(cts[0], outs[0])
+    chain_step = lambda s: ch.run(cts[s % RING], outs[s % RING])
+    for w in range(args.warmup):
+        chain_step(w)
+    with Clocks(local) as clk:
+        ms, launches = timed(chain_step, args.steps)
+    clocks = clk.summary()
+    value = args.steps * world / (ms / 1e3)
+
+    # ---- batched NTT of the digits (the dominant kernel) and the per-call split
+    ntt_step = lambda s: capi.call("heal_ntt", ch.dig_flat, ch.dev["p_t"], ch.dev["perm"], ch.dev["tw_t"],
+                                   None, None, ch.dn)
+    for w in range(3):
+        ntt_step(w)
+    ntt_ms, ntt_launches = timed(ntt_step, args.steps)
+    ntt_call_ms = ntt_ms / args.steps
+    limbs_per_call = 2 * L * D
+    ntt_bytes = 2 * limbs_per_call * N * 8           # read + write of every limb once
+    hbm, peak_kind = peaks()
+    achieved = ntt_bytes / (ntt_call_ms / 1e3) / 1e9
+    traffic = profile_traffic()
+    chain_bytes = ch.bytes_per_chain()
+
+    # ---- end to end through the C ABI from pinned host memory
+    nbytes = 2 * N * L * 8
+    import ctypes
+    pin_in, pin_out = ctypes.c_void_p(), ctypes.c_void_p()
+    capi.check(capi.lib().heal_host_alloc(nbytes, ctypes.byref(pin_in)))
+    capi.check(capi.lib().heal_host_alloc(nbytes, ctypes.byref(pin_out)))
+    ctypes.memmove(pin_in, cts_host[0].ctypes.data, nbytes)
+    dev_in, dev_out = cts[0], outs[0]
+
+    def e2e_step(s):
+        capi.check(capi.lib().heal_h2d_async(ctypes.c_void_p(dev_in.ptr), pin_in, nbytes))
+        ch.run(dev_in, dev_out)
+        capi.check(capi.lib().heal_d2h_async(pin_out, ctypes.c_void_p(dev_out.ptr), nbytes))
+
+    for w in range(args.warmup):
+        e2e_step(w)
+    e2e_ms, _ = timed(e2e_step, args.steps)
+    e2e = args.steps * world / (e2e_ms / 1e3)
+    got = np.frombuffer((ctypes.c_char * nbytes).from_address(pin_out.value), dtype=np.int64).reshape(ch.shape())
+    want = outs[0].numpy()
+    assert np.array_equal(got, want), "e2e output differs from the resident run"
+    capi.lib().heal_host_free(pin_in)
+    capi.lib().heal_host_free(pin_out)
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if world == 1 and not args.skip_cpu:
+        v, threads, runs = cpu_sample(ch.host, cts_host[0], seconds=args.cpu_seconds)
+        cpu = {"value": v, "unit": "chains/s", "cores": threads, "kind": "port",
+               "sample": f"CPU oracle chain on {SAMPLE_LIMBS} of the 24 limbs per run ({runs} runs, "
+                         f"~{args.cpu_seconds:.0f} s), scaled by {SAMPLE_LIMBS}/24"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "chains/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+                "config": CONFIG,
+                "ntt_limbs_per_s": limbs_per_call * args.steps * world / (ntt_ms / 1e3),
+                "chain_hbm_frac": chain_bytes * value / world / 1e9 / hbm,
+                "roofline": {"bound": "hbm", "kernel": "heal_ntt of the 72 digit limbs ([2, 65536, 1, 72] int64)",
+                             "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                             "frac": achieved / hbm, "algorithmic_bytes": ntt_bytes,
+                             "ms_per_call": ntt_call_ms,
+                             "traffic": traffic.get("bytes_per_call") if traffic else None},
+                "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+                "gpu_launches": launches, "launches_per_step": launches / args.steps,
+                "clocks": clocks, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

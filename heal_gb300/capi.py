@@ -1,0 +1,243 @@
+"""ctypes binding of the C ABI in include/heal_gb300.h.
+
+This is the binding a Python host would add for the backend (the same calls
+a cgo / JNI / N-API binding makes); the parity tests and bench.py drive the
+GPU through it.  `DeviceArray` is a strided view of HBM owned by the
+backend's allocator, the C-ABI counterpart of HEAL's DeviceTensor.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libheal_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "heal_gb300.h")
+MAX_DIMS = 8
+DTYPES = {np.dtype(np.int32): 0, np.dtype(np.int64): 1, np.dtype(np.float64): 2}
+NP_OF = {v: k for k, v in DTYPES.items()}
+
+
+class Tensor(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int32), ("ndim", ctypes.c_int32),
+                ("dims", ctypes.c_int64 * MAX_DIMS), ("strides", ctypes.c_int64 * MAX_DIMS)]
+
+
+_P = ctypes.POINTER(Tensor)
+_I64, _U64, _I32, _VP, _SZ = ctypes.c_int64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t
+SIGNATURES = {
+    "heal_init": ([ctypes.c_int], ctypes.c_int),
+    "heal_last_error": ([], ctypes.c_char_p),
+    "heal_synchronize": ([], ctypes.c_int),
+    "heal_get_stream": ([], _VP),
+    "heal_set_stream": ([_VP], ctypes.c_int),
+    "heal_kernel_launch_count": ([], _U64),
+    "heal_alloc": ([_SZ, ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
+    "heal_free": ([_VP], ctypes.c_int),
+    "heal_h2d": ([_VP, _VP, _SZ], ctypes.c_int),
+    "heal_d2h": ([_VP, _VP, _SZ], ctypes.c_int),
+    "heal_h2d_async": ([_VP, _VP, _SZ], ctypes.c_int),
+    "heal_d2h_async": ([_VP, _VP, _SZ], ctypes.c_int),
+    "heal_host_alloc": ([_SZ, ctypes.POINTER(_VP)], ctypes.c_int),
+    "heal_host_free": ([_VP], ctypes.c_int),
+    "heal_mark_modified": ([_VP], ctypes.c_int),
+    "heal_copy_strided": ([_P, _P], ctypes.c_int),
+    "heal_tensor_reshape": ([_P, _I32, ctypes.POINTER(_I64)], ctypes.c_int),
+    "heal_tensor_expand": ([_P, _I64, _I64], ctypes.c_int),
+    "heal_tensor_squeeze": ([_P, _I64], ctypes.c_int),
+    "heal_tensor_unsqueeze": ([_P, _I64], ctypes.c_int),
+    "heal_tensor_moveaxis": ([_P, _I64, _I64], ctypes.c_int),
+    "heal_tensor_slice": ([_P, _I64, _I64, _I64, _I64], ctypes.c_int),
+    "heal_tensor_is_contiguous": ([_P], ctypes.c_int),
+    "heal_tensor_span": ([_P], _I64),
+    "heal_modmul_ttt": ([_P, _P, _P, _P], ctypes.c_int),
+    "heal_modmul_ttc": ([_P, _P, _I64, _P], ctypes.c_int),
+    "heal_modmul_tct": ([_P, _I64, _P, _P], ctypes.c_int),
+    "heal_modmul_tcc": ([_P, _I64, _I64, _P], ctypes.c_int),
+    "heal_modsum_ttt": ([_P, _P, _P, _P], ctypes.c_int),
+    "heal_modsum_ttc": ([_P, _P, _I64, _P], ctypes.c_int),
+    "heal_modsum_tct": ([_P, _I64, _P, _P], ctypes.c_int),
+    "heal_modsum_tcc": ([_P, _I64, _I64, _P], ctypes.c_int),
+    "heal_mod_tt": ([_P, _P, _P], ctypes.c_int),
+    "heal_mod_tc": ([_P, _I64, _P], ctypes.c_int),
+    "heal_mod_ct": ([_I64, _P, _P], ctypes.c_int),
+    "heal_modneg_tt": ([_P, _P, _P], ctypes.c_int),
+    "heal_modneg_tc": ([_P, _I64, _P], ctypes.c_int),
+    "heal_axis_modsum": ([_P, _P, _P, _I64], ctypes.c_int),
+    "heal_g_decomposition": ([_P, _P, _U64, _U64], ctypes.c_int),
+    "heal_ntt": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "heal_intt": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "heal_permute": ([_P, _P, _P, _I64, _I64], ctypes.c_int),
+}
+
+
+def declared_symbols(header: str = HEADER) -> list[str]:
+    """Names of the functions include/heal_gb300.h declares."""
+    text = open(header).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*|void \*|uint64_t|int64_t)\s*\*?(heal_\w+)\(",
+                                 text, re.M)))
+
+
+_lib = None
+
+
+def lib():
+    """The loaded C ABI; raises if the CUDA extension has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build the backend first (heal_gb300.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+class HealError(RuntimeError):
+    pass
+
+
+_EXC = {1: ValueError, 2: IndexError, 3: RuntimeError, 4: MemoryError, 5: RuntimeError}
+
+
+def check(rc: int):
+    if rc:
+        raise _EXC.get(rc, HealError)(lib().heal_last_error().decode())
+
+
+def desc(data, dtype, shape, strides) -> Tensor:
+    t = Tensor()
+    t.data = data
+    t.dtype = DTYPES[np.dtype(dtype)]
+    t.ndim = len(shape)
+    for i in range(MAX_DIMS):
+        t.dims[i] = shape[i] if i < len(shape) else 1
+        t.strides[i] = strides[i] if i < len(shape) else 0
+    return t
+
+
+def _rowmajor(shape):
+    s, out = 1, []
+    for d in reversed(shape):
+        out.append(s)
+        s *= d
+    return tuple(reversed(out))
+
+
+class Buffer:
+    """One heal_alloc allocation, freed when the last view drops it."""
+
+    def __init__(self, nbytes: int, zero: bool = True):
+        self.ptr = ctypes.c_void_p()
+        self.nbytes = nbytes
+        if nbytes:
+            check(lib().heal_alloc(nbytes, 1 if zero else 0, ctypes.byref(self.ptr)))
+
+    def __del__(self):
+        if self.ptr and self.ptr.value and _lib is not None:
+            _lib.heal_free(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+
+class DeviceArray:
+    """A strided view (shape, strides in elements, byte offset) of a Buffer."""
+
+    def __init__(self, buf: Buffer, dtype, shape, strides=None, offset: int = 0):
+        self.buf = buf
+        self.dtype = np.dtype(dtype)
+        self.shape = tuple(int(s) for s in shape)
+        self.strides = tuple(int(s) for s in (strides if strides is not None else _rowmajor(self.shape)))
+        self.offset = offset
+
+    # ---- construction
+    @classmethod
+    def empty(cls, shape, dtype, zero: bool = True) -> "DeviceArray":
+        n = int(np.prod(shape)) if len(shape) else 1
+        return cls(Buffer(n * np.dtype(dtype).itemsize, zero), dtype, shape)
+
+    @classmethod
+    def from_numpy(cls, arr: np.ndarray) -> "DeviceArray":
+        """Upload keeping the array's strides, as HEAL's host_to_device does."""
+        arr = np.asarray(arr)
+        if arr.dtype not in DTYPES:
+            raise TypeError(f"unsupported dtype {arr.dtype}")
+        st = tuple(s // arr.itemsize for s in arr.strides)
+        if any(s < 0 for s in st):
+            arr = np.ascontiguousarray(arr)
+            st = tuple(s // arr.itemsize for s in arr.strides)
+        span = 0 if arr.size == 0 else 1 + sum((d - 1) * s for d, s in zip(arr.shape, st))
+        buf = Buffer(span * arr.itemsize, zero=False)
+        if span:
+            check(lib().heal_h2d(buf.ptr, ctypes.c_void_p(arr.ctypes.data), span * arr.itemsize))
+        return cls(buf, arr.dtype, arr.shape, st)
+
+    # ---- access
+    @property
+    def ptr(self) -> int:
+        return (self.buf.ptr.value or 0) + self.offset
+
+    @property
+    def size(self) -> int:
+        return int(np.prod(self.shape)) if self.shape else 1
+
+    def desc(self) -> Tensor:
+        return desc(self.ptr if self.buf.ptr.value else None, self.dtype, self.shape, self.strides)
+
+    def numpy(self) -> np.ndarray:
+        n = self.size
+        if n == 0:
+            check(lib().heal_synchronize())
+            return np.zeros(self.shape, self.dtype)
+        span = 1 + sum((d - 1) * s for d, s in zip(self.shape, self.strides))
+        host = np.empty(span, self.dtype)
+        check(lib().heal_d2h(ctypes.c_void_p(host.ctypes.data), ctypes.c_void_p(self.ptr), span * self.dtype.itemsize))
+        view = np.lib.stride_tricks.as_strided(host, self.shape, [s * self.dtype.itemsize for s in self.strides])
+        return np.array(view)
+
+    def _meta(self, fn, *args) -> "DeviceArray":
+        d = self.desc()
+        check(fn(ctypes.byref(d), *args))
+        nd = d.ndim
+        off = (d.data or 0) - (self.buf.ptr.value or 0) if d.data else self.offset
+        return DeviceArray(self.buf, self.dtype, list(d.dims)[:nd], list(d.strides)[:nd], off)
+
+    def reshape(self, shape) -> "DeviceArray":
+        arr = (_I64 * len(shape))(*shape)
+        return self._meta(lib().heal_tensor_reshape, len(shape), arr)
+
+    def moveaxis(self, src: int, dst: int) -> "DeviceArray":
+        return self._meta(lib().heal_tensor_moveaxis, src, dst)
+
+    def expand(self, axis: int, repeats: int) -> "DeviceArray":
+        return self._meta(lib().heal_tensor_expand, axis, repeats)
+
+
+def _arg(x):
+    if x is None:
+        return None
+    if isinstance(x, DeviceArray):
+        return ctypes.byref(x.desc())
+    return x
+
+
+def call(name: str, *args):
+    """Calls C-ABI function `name`, passing DeviceArrays as descriptors."""
+    check(getattr(lib(), name)(*[_arg(a) for a in args]))
+
+
+def synchronize():
+    check(lib().heal_synchronize())
+
+
+def launches() -> int:
+    return int(lib().heal_kernel_launch_count())
+
+
+def stream() -> int:
+    return int(lib().heal_get_stream() or 0)

@@ -1,0 +1,97 @@
+"""The keyswitch-shaped chain as a sequence of HEAL calls on the GPU.
+
+One step, on a ciphertext tensor ct[2, N, 1, L] (HEAL's [l, m, r, k] with
+the 2 ciphertext components as l and the L RNS limbs as k):
+
+  x     = intt(ct)                                   [2, N, 1, L]
+  dig   = g_decomposition(x, D, base_bits)           [2, N, 1, L, D]
+  dn    = ntt(dig viewed [2, N, 1, L*D], moduli tiled D times)
+  prod  = modmul_ttt(dn, key[2, N, 1, L*D], moduli tiled)
+  acc   = axis_modsum(prod viewed [2, N, 1, D, L], p, axis=3)
+  out   = permute(acc, galois[1, N], elementwise_axis=2, perm_axis=1)
+
+Every step is one C-ABI call (include/heal_gb300.h); the reshape and the
+digit-axis move are stride-only views.  The moduli are the L largest primes
+q < 2^bound_bits with q = 1 (mod 2N); the key is seeded uniform residues; the
+Galois map is X -> X^(5^r mod 2N).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import capi
+from . import params as P
+
+
+class KeyswitchChain:
+    def __init__(self, n: int = 1 << 16, limbs: int = 24, digits: int = 3, base_bits: int = 17,
+                 bound_bits: int = 50, rot: int = 1, key_seed: int = 7, dtype=np.int64):
+        self.n, self.L, self.D, self.bits = n, limbs, digits, base_bits
+        self.dtype = np.dtype(dtype)
+        qs = P.ntt_primes(1 << bound_bits, n, limbs)
+        self.qs = qs
+        p, perm, tw, itw, minv = P.ntt_tables(qs, n, self.dtype)
+        self.host = {"p": p, "perm": perm, "tw": tw, "itw": itw, "minv": minv}
+        self.host["p_t"] = np.repeat(p, digits)
+        self.host["tw_t"] = np.repeat(tw, digits, axis=0)
+        self.host["key"] = P.residues(key_seed, (2, n, 1, limbs * digits), self.host["p_t"], self.dtype)
+        elt = pow(5, rot, 2 * n)
+        self.host["gal"] = P.galois_perm(n, elt).reshape(1, n).astype(self.dtype)
+        D = capi.DeviceArray.from_numpy
+        self.dev = {k: D(v) for k, v in self.host.items()}
+        E = capi.DeviceArray.empty
+        self.x = E((2, n, 1, limbs), self.dtype, zero=False)
+        self.dig = E((2, n, 1, limbs, digits), self.dtype, zero=False)
+        self.dn = E((2, n, 1, limbs * digits), self.dtype, zero=False)
+        self.acc = E((2, n, 1, limbs), self.dtype, zero=False)
+        self.dig_flat = self.dig.reshape((2, n, 1, limbs * digits))
+        self.prod_moved = self.dn.reshape((2, n, 1, limbs, digits)).moveaxis(4, 3)
+
+    def shape(self):
+        return (2, self.n, 1, self.L)
+
+    def run(self, ct: capi.DeviceArray, out: capi.DeviceArray):
+        """Enqueues one chain step (6 HEAL calls) on the library stream."""
+        d = self.dev
+        capi.call("heal_intt", ct, d["p"], d["perm"], d["itw"], d["minv"], None, None, self.x)
+        capi.call("heal_g_decomposition", self.x, self.dig, self.D, self.bits)
+        capi.call("heal_ntt", self.dig_flat, d["p_t"], d["perm"], d["tw_t"], None, None, self.dn)
+        capi.call("heal_modmul_ttt", self.dn, d["key"], d["p_t"], self.dn)
+        capi.call("heal_axis_modsum", self.prod_moved, d["p"], self.acc, 3)
+        capi.call("heal_permute", self.acc, d["gal"], out, 2, 1)
+
+    # ---- algorithmic bytes (reads + writes of the six calls, tables excluded)
+    def bytes_per_chain(self) -> int:
+        e = self.dtype.itemsize
+        ct = 2 * self.n * self.L * e
+        dg = ct * self.D
+        return (2 * ct) + (ct + dg) + (2 * dg) + (3 * dg) + (dg + ct) + (2 * ct)
+
+    def ntt_limbs_per_chain(self) -> int:
+        return 2 * self.L + 2 * self.L * self.D
+
+
+def oracle_chain(ch_host: dict, ct: np.ndarray, digits: int, base_bits: int, limb_idx=None):
+    """The same chain on the CPU oracle (tests / bench baseline only).  With
+    `limb_idx`, only those limbs are computed: every output limb depends only
+    on its own input limb and key columns."""
+    from oracle import oracle as O
+    h = ch_host
+    p, perm, tw, itw, minv = h["p"], h["perm"], h["tw"], h["itw"], h["minv"]
+    key = h["key"]
+    L = len(p)
+    if limb_idx is not None:
+        li = np.asarray(limb_idx)
+        cols = (li[:, None] * digits + np.arange(digits)[None, :]).reshape(-1)
+        p, tw, itw, minv = p[li], tw[li], itw[li], minv[li]
+        key = key[..., cols]
+        ct = ct[..., li]
+        L = len(li)
+    x = O.intt(np.ascontiguousarray(ct), p, perm, itw, minv)
+    dig, _ = O.g_decomposition(x, digits, base_bits)
+    n = ct.shape[1]
+    p_t = np.repeat(p, digits)
+    dn = O.ntt(dig.reshape(2, n, 1, L * digits), p_t, perm, np.repeat(tw, digits, axis=0))
+    prod = O.modmul(dn, np.ascontiguousarray(key), p_t)
+    acc = O.axis_modsum(np.moveaxis(prod.reshape(2, n, 1, L, digits), 4, 3), p, 3)
+    return O.permute(acc, h["gal"], 2, 1)

@@ -1,0 +1,460 @@
+// heal_modop.cu — elementwise modular arithmetic with broadcasting:
+// modmul / modsum (HEAL include/modop.h:47-111), mod (modop.h:115-134) and
+// the modneg extension, over int32 and int64 tensors of any strides.
+//
+// Semantics follow example_impl/modop_impl.cpp: for every coordinate of
+// `result`, res = (T)((T_DP)a op (T_DP)b % (T_DP)p) with C's truncating `%`,
+// operands read with at_with_broadcast (right-aligned, index 0 on size-1
+// axes).  Non-negative operands with a positive modulus take the fast paths
+// of heal_arith.h; anything else takes the exact double-width `%`.
+//
+// Two kernels: a dense kernel (result, a and b row-major with the same
+// shape, p a scalar or a [k] vector on the last axis — every call of the
+// keyswitch chain) that streams 16-byte vectors, and a general strided
+// kernel.  Both are HBM-bound: per element they move sizeof(T) x (reads of
+// a and b + one write).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <type_traits>
+#include <cstring>
+
+#include "heal_internal.h"
+
+namespace heal {
+
+enum Op { OP_MUL = 0, OP_SUM = 1, OP_NEG = 2, OP_MOD = 3 };
+
+struct ModopArgs {
+  View a, b, p, r;  // views in result coordinates (stride 0 on broadcast axes)
+  View pd;          // result coordinate -> dense index into the modulus table
+  const void *ap, *bp, *pp;
+  void *rp;
+  int64_t bs, ps;      // scalars when bp / pp are null
+  const void *ptab;    // MG32 / MG64 per modulus element, or null
+  MG64 pc64;           // scalar-modulus constants
+  MG32 pc32;
+  int64_t n;
+  int64_t last;        // result's last dimension (dense kernel)
+  FastDiv last_div;    // division by `last` (dense kernel, n < 2^32)
+  int p_per_last;      // dense kernel: modulus index = coordinate on the last axis
+  Diag *diag;
+};
+
+// ------------------------------------------------------------ element op
+template <typename T> struct MGOf;
+template <> struct MGOf<int32_t> { typedef MG32 type; };
+template <> struct MGOf<int64_t> { typedef MG64 type; };
+
+template <typename T, int OP>
+__device__ __forceinline__ T elem_op(int64_t a, int64_t b, int64_t p, const typename MGOf<T>::type &c, Diag *diag) {
+  if (OP == OP_MOD) {  // (T)(a % b) in T; p unused
+    if (b == 0) {
+      atomicAdd(&diag->zero_mod, 1ull);
+      return 0;
+    }
+    if (b == -1) return 0;
+    return (T)(a % b);
+  }
+  if (p == 0) {
+    atomicAdd(&diag->zero_mod, 1ull);
+    return 0;
+  }
+  if (OP == OP_MUL) {
+    if (a >= 0 && b >= 0 && p > 0) {
+      if (sizeof(T) == 4) return (T)mg32_mod((uint64_t)a * (uint64_t)b, (const MG32 &)c);
+      return (T)mg64_mulmod((uint64_t)a, (uint64_t)b, (const MG64 &)c);
+    }
+    return (T)((i128)a * (i128)b % (i128)p);
+  }
+  if (OP == OP_SUM) {
+    if (a >= 0 && b >= 0 && p > 0) {
+      uint64_t x = (uint64_t)a + (uint64_t)b;
+      if (a < p && b < p) return (T)(x >= (uint64_t)p ? x - (uint64_t)p : x);
+      return (T)(x % (uint64_t)p);
+    }
+    return (T)(((i128)a + (i128)b) % (i128)p);
+  }
+  // OP_NEG: (p - a % p) % p
+  if (a >= 0 && p > 0) {
+    int64_t t = a < p ? a : a % p;
+    return (T)(t ? p - t : 0);
+  }
+  i128 t = (i128)a % (i128)p;
+  return (T)(((i128)p - t) % (i128)p);
+}
+
+// modulus constants and value of modulus element `idx` (table) or the scalar
+template <typename T>
+__device__ __forceinline__ typename MGOf<T>::type mg_of(const ModopArgs &g, int64_t idx) {
+  typedef typename MGOf<T>::type M;
+  if (g.ptab) return ((const M *)g.ptab)[idx];
+  if (sizeof(T) == 4) {
+    MG32 c = g.pc32;
+    return *(const M *)&c;
+  }
+  MG64 c = g.pc64;
+  return *(const M *)&c;
+}
+template <typename T>
+__device__ __forceinline__ int64_t q_of(const ModopArgs &g, const typename MGOf<T>::type &c) {
+  if (!g.ptab) return g.ps;
+  return sizeof(T) == 4 ? (int64_t)(int32_t)c.q : (int64_t)c.q;
+}
+
+template <typename T>
+struct VecOf {
+  typedef typename std::conditional<sizeof(T) == 8, longlong2, int4>::type type;
+};
+
+// ------------------------------------------------------ dense kernel
+// result, a (and b) row-major with result's shape; VEC elements per step.
+template <typename T, int OP, int VEC>
+__global__ void __launch_bounds__(256) modop_dense_kernel(const __grid_constant__ ModopArgs g) {
+  typedef typename VecOf<T>::type V;
+  const T *A = (const T *)g.ap;
+  const T *B = (const T *)g.bp;
+  T *R = (T *)g.rp;
+  const int64_t nvec = g.n / VEC;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t base = v * VEC;
+    T av[VEC], bv[VEC], rv[VEC];
+    if (VEC == 1) {
+      av[0] = A[base];
+      if (B) bv[0] = B[base];
+    } else {
+      *(V *)av = __ldcs((const V *)(A + base));
+      if (B) *(V *)bv = __ldcs((const V *)(B + base));
+    }
+    uint32_t col = 0;
+    if (g.p_per_last) col = (uint32_t)base - fastdiv((uint32_t)base, g.last_div) * (uint32_t)g.last;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+      typename MGOf<T>::type c = mg_of<T>(g, col);
+      int64_t b = B ? (int64_t)bv[j] : g.bs;
+      rv[j] = elem_op<T, OP>((int64_t)av[j], b, q_of<T>(g, c), c, g.diag);
+      if (g.p_per_last && ++col == (uint32_t)g.last) col = 0;
+    }
+    if (VEC == 1) {
+      R[base] = rv[0];
+    } else {
+      __stcs((V *)(R + base), *(const V *)rv);
+    }
+  }
+  // tail (n not a multiple of VEC)
+  if (VEC > 1 && blockIdx.x == 0 && (int64_t)threadIdx.x < g.n % VEC) {
+    int64_t i = nvec * VEC + threadIdx.x;
+    int64_t col = g.p_per_last ? i % g.last : 0;
+    typename MGOf<T>::type c = mg_of<T>(g, col);
+    int64_t b = B ? (int64_t)B[i] : g.bs;
+    R[i] = elem_op<T, OP>((int64_t)A[i], b, q_of<T>(g, c), c, g.diag);
+  }
+}
+
+// ---------------------------------------------------- general kernel
+template <typename T, int OP>
+__global__ void __launch_bounds__(256) modop_general_kernel(const __grid_constant__ ModopArgs g) {
+  const T *A = (const T *)g.ap;
+  const T *B = (const T *)g.bp;
+  const T *P = (const T *)g.pp;
+  T *R = (T *)g.rp;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = idx, oa = 0, ob = 0, op = 0, orr = 0, opd = 0;
+    for (int i = g.r.ndim - 1; i >= 0; --i) {
+      int64_t d = g.r.dims[i];
+      int64_t c = rem % d;
+      rem /= d;
+      oa += c * g.a.strides[i];
+      ob += c * g.b.strides[i];
+      op += c * g.p.strides[i];
+      opd += c * g.pd.strides[i];
+      orr += c * g.r.strides[i];
+    }
+    typename MGOf<T>::type c = mg_of<T>(g, opd);
+    int64_t p = P ? (int64_t)P[op] : g.ps;
+    int64_t b = B ? (int64_t)B[ob] : g.bs;
+    R[orr] = elem_op<T, OP>((int64_t)A[oa], b, p, c, g.diag);
+  }
+}
+
+// ----------------------------------------------------------- host side
+static int grid_for(int64_t work, int threads, int per_sm) {
+  int64_t want = (work + threads - 1) / threads;
+  int64_t cap = (int64_t)std::max(device_sm_count(), 1) * per_sm;
+  return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+// View of `t` in the coordinates of `r` (right-aligned, stride 0 on size-1
+// axes, as at_with_broadcast reads it).
+static View bcast_view(const heal_tensor &t, const heal_tensor &r) {
+  View v = make_view(r);
+  int off = r.ndim - t.ndim;
+  for (int j = 0; j < r.ndim; ++j) {
+    int i = j - off;
+    v.strides[j] = (i < 0 || t.dims[i] == 1) ? 0 : t.strides[i];
+  }
+  return v;
+}
+
+// dense row-major strides of `t` mapped into r's coordinates
+static View bcast_dense_view(const heal_tensor &t, const heal_tensor &r) {
+  heal_tensor d = t;
+  int64_t s = 1;
+  for (int i = t.ndim - 1; i >= 0; --i) {
+    d.strides[i] = s;
+    s *= t.dims[i];
+  }
+  return bcast_view(d, r);
+}
+
+static bool dense_rowmajor(const heal_tensor &t) {
+  int64_t s = 1;
+  for (int i = t.ndim - 1; i >= 0; --i) {
+    if (t.dims[i] != 1 && t.strides[i] != s) return false;
+    s *= t.dims[i];
+  }
+  return true;
+}
+
+static int check_bcast(const heal_tensor &t, const heal_tensor &r, const char *label) {
+  // CHECK_DIMS_BROADCASTABLE (modop_impl.cpp:89-101)
+  if (t.ndim > r.ndim) return set_error(HEAL_ERR_INVALID_ARGUMENT, std::string(label) + " has more dims than result.");
+  for (int i = 1; i <= t.ndim; ++i) {
+    int64_t td = t.dims[t.ndim - i], rd = r.dims[r.ndim - i];
+    if (td != 1 && td != rd)
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, std::string(label) + " not broadcast-compatible with result.");
+  }
+  return HEAL_OK;
+}
+
+static int check_p(const heal_tensor &p, const heal_tensor &r) {
+  // CHECK_DIMS_MATCH_LAST (modop_impl.cpp:84-87), then the bounds at() applies
+  // to at_with_broadcast's indices (device_memory_impl.cpp:100-103,116-124).
+  if (p.ndim != 1 && (p.ndim == 0 || r.ndim == 0 || p.dims[p.ndim - 1] != r.dims[r.ndim - 1]))
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "Last dimension of p must match last dimension of result.");
+  if (p.ndim > r.ndim) return set_error(HEAL_ERR_INVALID_ARGUMENT, "p has more dims than result.");
+  if (numel(r) == 0) return HEAL_OK;
+  int off = r.ndim - p.ndim;
+  for (int i = 0; i < p.ndim; ++i)
+    if (p.dims[i] != 1 && p.dims[i] < r.dims[i + off]) return set_error(HEAL_ERR_OUT_OF_RANGE, "Index out of bounds.");
+  return HEAL_OK;
+}
+
+template <typename T, int OP>
+static int launch(ModopArgs &g, bool dense) {
+  cudaStream_t s = stream();
+  if (dense) {
+    const int vec = 16 / sizeof(T);
+    bool aligned = ((uintptr_t)g.ap % 16 == 0) && ((uintptr_t)g.rp % 16 == 0) && (!g.bp || (uintptr_t)g.bp % 16 == 0);
+    if (aligned) {
+      modop_dense_kernel<T, OP, 16 / sizeof(T)><<<grid_for(g.n / vec + 1, 256, 8), 256, 0, s>>>(g);
+    } else {
+      modop_dense_kernel<T, OP, 1><<<grid_for(g.n, 256, 8), 256, 0, s>>>(g);
+    }
+  } else {
+    modop_general_kernel<T, OP><<<grid_for(g.n, 256, 8), 256, 0, s>>>(g);
+  }
+  return check_launch("modop");
+}
+
+// a, b (tensor or scalar), p (tensor or scalar) -> result
+static int modop(int op, const heal_tensor *a, const heal_tensor *b, int64_t bs, const heal_tensor *p, int64_t ps,
+                 const heal_tensor *r) {
+  clear_error();
+  HEAL_CHECK(check_desc(a, "a", true));
+  if (b) HEAL_CHECK(check_desc(b, "b", true));
+  if (p) HEAL_CHECK(check_desc(p, "p", true));
+  HEAL_CHECK(check_desc(r, "result", true));
+  HEAL_CHECK(ensure_init());
+  const int dt = r->dtype;
+  if (a->dtype != dt || (b && b->dtype != dt) || (p && p->dtype != dt))
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "all tensors must have the element type of result");
+  if (op == OP_MOD) {
+    // CHECK_SAME_DIMS (modop_impl.cpp:183-186)
+    if (!same_dims(*a, *r)) return set_error(HEAL_ERR_INVALID_ARGUMENT, "a must have exactly the same shape as result.");
+    if (b && !same_dims(*b, *r))
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "b must have exactly the same shape as result.");
+  } else {
+    HEAL_CHECK(check_bcast(*a, *r, "a"));
+    if (b) HEAL_CHECK(check_bcast(*b, *r, "b"));
+    if (p) HEAL_CHECK(check_p(*p, *r));
+  }
+  const int64_t n = numel(*r);
+  if (n == 0) return HEAL_OK;
+
+  // inputs that overlap the result in another layout are copied first
+  heal_tensor A = *a, B = b ? *b : heal_tensor(), P = p ? *p : heal_tensor();
+  void *owned[3] = {nullptr, nullptr, nullptr};
+  auto detach = [&](heal_tensor &t, int slot) -> int {
+    if (overlaps(t, *r) && !identical_view(t, *r)) return materialize(t, &t, &owned[slot]);
+    return HEAL_OK;
+  };
+  int rc = detach(A, 0);
+  if (!rc && b) rc = detach(B, 1);
+  if (!rc && p) rc = detach(P, 2);
+
+  ModopArgs g;
+  memset(&g, 0, sizeof g);
+  if (!rc) {
+    g.r = make_view(*r);
+    g.a = bcast_view(A, *r);
+    g.b = b ? bcast_view(B, *r) : make_view(*r);
+    g.p = p ? bcast_view(P, *r) : make_view(*r);
+    g.pd = p ? bcast_dense_view(P, *r) : make_view(*r);
+    if (!b)
+      for (int i = 0; i < HEAL_MAX_DIMS; ++i) g.b.strides[i] = 0;
+    if (!p)
+      for (int i = 0; i < HEAL_MAX_DIMS; ++i) g.p.strides[i] = g.pd.strides[i] = 0;
+    g.ap = A.data;
+    g.bp = b ? B.data : nullptr;
+    g.pp = p ? P.data : nullptr;
+    g.rp = r->data;
+    g.bs = dt == HEAL_INT32 ? (int64_t)(int32_t)bs : bs;
+    g.ps = dt == HEAL_INT32 ? (int64_t)(int32_t)ps : ps;
+    g.n = n;
+    g.diag = diag_device();
+    g.last = r->ndim ? r->dims[r->ndim - 1] : 1;
+    if (op != OP_MOD) {
+      if (p) {
+        ModTable mt;
+        rc = mod_table(P, &mt);
+        g.ptab = mt.consts;
+      } else {
+        g.pc64 = mg64_make(g.ps);
+        g.pc32 = mg32_make(g.ps);
+      }
+    }
+  }
+  if (!rc) {
+    // dense: result, a, b row-major with result's shape; p scalar or [k] on
+    // the last axis (k == last or broadcast 1)
+    bool dense = dense_rowmajor(*r) && same_dims(A, *r) && dense_rowmajor(A) &&
+                 (!b || (same_dims(B, *r) && dense_rowmajor(B))) && n < (int64_t)UINT32_MAX && r->ndim > 0;
+    if (dense && p) {
+      bool vec_last = P.ndim == 1 && (P.dims[0] == 1 || g.last <= P.dims[0]);
+      dense = vec_last && P.strides[0] == 1;
+      g.p_per_last = vec_last && P.dims[0] != 1;
+    }
+    if (dense && g.last > 0 && g.last < (int64_t)UINT32_MAX) g.last_div = fastdiv_make((uint32_t)g.last);
+    else dense = dense && !g.p_per_last;
+    if (op == OP_MOD) {
+      // mod_tt / tc / ct: a and b play the roles of dividend and divisor
+      rc = dt == HEAL_INT32 ? launch<int32_t, OP_MOD>(g, dense) : launch<int64_t, OP_MOD>(g, dense);
+    } else if (dt == HEAL_INT32) {
+      rc = op == OP_MUL ? launch<int32_t, OP_MUL>(g, dense)
+           : op == OP_SUM ? launch<int32_t, OP_SUM>(g, dense) : launch<int32_t, OP_NEG>(g, dense);
+    } else {
+      rc = op == OP_MUL ? launch<int64_t, OP_MUL>(g, dense)
+           : op == OP_SUM ? launch<int64_t, OP_SUM>(g, dense) : launch<int64_t, OP_NEG>(g, dense);
+    }
+  }
+  for (void *o : owned) scratch_free(o);
+  if (!rc) mark_written(r->data);
+  return rc;
+}
+
+// mod_ct: scalar dividend, tensor divisor — run as a general kernel over b
+static int mod_ct(int64_t as, const heal_tensor *b, const heal_tensor *r) {
+  clear_error();
+  HEAL_CHECK(check_desc(b, "b", true));
+  HEAL_CHECK(check_desc(r, "result", true));
+  HEAL_CHECK(ensure_init());
+  if (b->dtype != r->dtype) return set_error(HEAL_ERR_INVALID_ARGUMENT, "all tensors must have the element type of result");
+  if (!same_dims(*b, *r)) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b must have exactly the same shape as result.");
+  const int64_t n = numel(*r);
+  if (n == 0) return HEAL_OK;
+  // a scalar broadcast as a stride-0 view over b's shape is the dividend
+  heal_tensor B = *b;
+  void *owned = nullptr;
+  if (overlaps(B, *r) && !identical_view(B, *r)) HEAL_CHECK(materialize(B, &B, &owned));
+  ModopArgs g;
+  memset(&g, 0, sizeof g);
+  g.r = make_view(*r);
+  g.b = make_view(B);
+  g.a = make_view(*r);
+  for (int i = 0; i < HEAL_MAX_DIMS; ++i) g.a.strides[i] = 0;
+  g.p = g.pd = g.a;
+  g.n = n;
+  g.diag = diag_device();
+  g.rp = r->data;
+  g.bp = B.data;
+  int rc;
+  // the dividend lives in a one-element device buffer
+  void *sbuf;
+  HEAL_CHECK(scratch_alloc(8, &sbuf));
+  int64_t v64 = as;
+  int32_t v32 = (int32_t)as;
+  rc = cudaMemcpyAsync(sbuf, r->dtype == HEAL_INT32 ? (const void *)&v32 : (const void *)&v64,
+                       elem_size(r->dtype), cudaMemcpyHostToDevice, stream()) == cudaSuccess
+           ? HEAL_OK
+           : set_error(HEAL_ERR_CUDA, "mod_ct: copy failed");
+  g.ap = sbuf;
+  if (!rc) rc = r->dtype == HEAL_INT32 ? launch<int32_t, OP_MOD>(g, false) : launch<int64_t, OP_MOD>(g, false);
+  scratch_free(sbuf);
+  scratch_free(owned);
+  if (!rc) mark_written(r->data);
+  return rc;
+}
+
+}  // namespace heal
+
+using namespace heal;
+
+extern "C" {
+
+int heal_modmul_ttt(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *r) {
+  if (!p) return set_error(HEAL_ERR_INVALID_ARGUMENT, "p pointer must not be null.");
+  if (!b) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b pointer must not be null.");
+  return modop(OP_MUL, a, b, 0, p, 0, r);
+}
+int heal_modmul_ttc(const heal_tensor *a, const heal_tensor *b, int64_t p, const heal_tensor *r) {
+  if (!b) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b pointer must not be null.");
+  return modop(OP_MUL, a, b, 0, nullptr, p, r);
+}
+int heal_modmul_tct(const heal_tensor *a, int64_t b, const heal_tensor *p, const heal_tensor *r) {
+  if (!p) return set_error(HEAL_ERR_INVALID_ARGUMENT, "p pointer must not be null.");
+  return modop(OP_MUL, a, nullptr, b, p, 0, r);
+}
+int heal_modmul_tcc(const heal_tensor *a, int64_t b, int64_t p, const heal_tensor *r) {
+  return modop(OP_MUL, a, nullptr, b, nullptr, p, r);
+}
+int heal_modsum_ttt(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *r) {
+  if (!p) return set_error(HEAL_ERR_INVALID_ARGUMENT, "p pointer must not be null.");
+  if (!b) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b pointer must not be null.");
+  return modop(OP_SUM, a, b, 0, p, 0, r);
+}
+int heal_modsum_ttc(const heal_tensor *a, const heal_tensor *b, int64_t p, const heal_tensor *r) {
+  if (!b) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b pointer must not be null.");
+  return modop(OP_SUM, a, b, 0, nullptr, p, r);
+}
+int heal_modsum_tct(const heal_tensor *a, int64_t b, const heal_tensor *p, const heal_tensor *r) {
+  if (!p) return set_error(HEAL_ERR_INVALID_ARGUMENT, "p pointer must not be null.");
+  return modop(OP_SUM, a, nullptr, b, p, 0, r);
+}
+int heal_modsum_tcc(const heal_tensor *a, int64_t b, int64_t p, const heal_tensor *r) {
+  return modop(OP_SUM, a, nullptr, b, nullptr, p, r);
+}
+int heal_modneg_tt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *r) {
+  if (!p) return set_error(HEAL_ERR_INVALID_ARGUMENT, "p pointer must not be null.");
+  return modop(OP_NEG, a, nullptr, 0, p, 0, r);
+}
+int heal_modneg_tc(const heal_tensor *a, int64_t p, const heal_tensor *r) {
+  return modop(OP_NEG, a, nullptr, 0, nullptr, p, r);
+}
+int heal_mod_tt(const heal_tensor *a, const heal_tensor *b, const heal_tensor *r) {
+  if (!a) return set_error(HEAL_ERR_INVALID_ARGUMENT, "a pointer must not be null.");
+  if (!b) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b pointer must not be null.");
+  return modop(OP_MOD, a, b, 0, nullptr, 0, r);
+}
+int heal_mod_tc(const heal_tensor *a, int64_t b, const heal_tensor *r) {
+  if (!a) return set_error(HEAL_ERR_INVALID_ARGUMENT, "a pointer must not be null.");
+  return modop(OP_MOD, a, nullptr, b, nullptr, 0, r);
+}
+int heal_mod_ct(int64_t a, const heal_tensor *b, const heal_tensor *r) {
+  if (!b) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b pointer must not be null.");
+  return mod_ct(a, b, r);
+}
+
+}  // extern "C"

@@ -1,0 +1,390 @@
+// heal_reduce.cu — axis_modsum, g_decomposition and permute.
+//
+//  axis_modsum   (HEAL include/axis_modsum.h:24-30; axis_modsum_impl.cpp)
+//                one thread per output element; the reduction runs in the
+//                reference's order, sum = (sum + a_r) % q, so negative
+//                operands give the same truncated residues.
+//  g_decomposition (include/g_decomposition.h:24-30; g_decomposition_impl.cpp)
+//                one thread per input element writes its `power` digits;
+//                `value % base` and `value /= base` act on the value converted
+//                to uint64 (base is a size_t), the quotient stored back in T.
+//  permute       (include/permute.h:33-40; permute_impl.cpp) a gather of
+//                whole rows along perm_axis.
+// All three are HBM-bound streams.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "heal_internal.h"
+
+namespace heal {
+
+static int grid_for(int64_t work, int threads, int per_sm) {
+  int64_t want = (work + threads - 1) / threads;
+  int64_t cap = (int64_t)std::max(device_sm_count(), 1) * per_sm;
+  return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+static bool dense_rowmajor(const heal_tensor &t) {
+  int64_t s = 1;
+  for (int i = t.ndim - 1; i >= 0; --i) {
+    if (t.dims[i] != 1 && t.strides[i] != s) return false;
+    s *= t.dims[i];
+  }
+  return true;
+}
+
+// ============================================================ axis_modsum
+struct AxisArgs {
+  View r;          // result view
+  View ai;         // a strides in result coordinates
+  int64_t ax_len, ax_stride;
+  int64_t p_stride;  // p stride, indexed by the last input coordinate
+  int last_from_axis;  // the last input coordinate is result's last one
+  const void *a, *p;
+  void *out;
+  int64_t n;
+  Diag *diag;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) axis_modsum_kernel(const __grid_constant__ AxisArgs g) {
+  const T *A = (const T *)g.a;
+  const T *P = (const T *)g.p;
+  T *R = (T *)g.out;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = idx, oa = 0, orr = 0, last = 0;
+    for (int i = g.r.ndim - 1; i >= 0; --i) {
+      int64_t d = g.r.dims[i];
+      int64_t c = rem % d;
+      rem /= d;
+      if (i == g.r.ndim - 1) last = c;
+      oa += c * g.ai.strides[i];
+      orr += c * g.r.strides[i];
+    }
+    const int64_t q = (int64_t)P[last * g.p_stride];
+    if (q == 0) {
+      atomicAdd(&g.diag->zero_mod, 1ull);
+      R[orr] = 0;
+      continue;
+    }
+    int64_t sum = 0;
+    for (int64_t k = 0; k < g.ax_len; ++k) {
+      int64_t v = (int64_t)A[oa + k * g.ax_stride];
+      if (sum >= 0 && v >= 0 && q > 0) {
+        uint64_t x = (uint64_t)sum + (uint64_t)v;
+        sum = v < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
+      } else {
+        sum = crem128((i128)sum + (i128)v, q);
+      }
+    }
+    R[orr] = (T)sum;
+  }
+}
+
+static int axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_tensor *r, int64_t axis) {
+  clear_error();
+  HEAL_CHECK(check_desc(a, "a", true));
+  HEAL_CHECK(check_desc(p, "p", true));
+  HEAL_CHECK(check_desc(r, "result", true));
+  HEAL_CHECK(ensure_init());
+  if (a->dtype != r->dtype || p->dtype != r->dtype)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "all tensors must have the element type of result");
+  // axis_modsum_impl.cpp:19-33
+  if (p->ndim != 1) return set_error(HEAL_ERR_INVALID_ARGUMENT, "p must be a 1D tensor of shape [k]");
+  const int nd = a->ndim;
+  if (axis < 0 || axis >= nd - 1)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "axis must be in range [0, ndim - 2] (can't reduce across last axis)");
+  if (a->dims[nd - 1] != p->dims[0])
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "Last dimension of a must match shape of p");
+  if (r->ndim != nd - 1)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "Result must have the shape of a with the reduced axis removed.");
+  const int64_t n = numel(*r);
+  for (int i = 0, j = 0; i < nd; ++i) {
+    if (i == axis) continue;
+    if (n > 0 && r->dims[j] > a->dims[i]) return set_error(HEAL_ERR_OUT_OF_RANGE, "Index out of bounds.");
+    ++j;
+  }
+  if (n == 0) return HEAL_OK;
+  heal_tensor A = *a, P = *p;
+  void *oa = nullptr, *op = nullptr;
+  int rc = HEAL_OK;
+  if (overlaps(A, *r)) rc = materialize(A, &A, &oa);
+  if (!rc && overlaps(P, *r)) rc = materialize(P, &P, &op);
+  if (!rc) {
+    AxisArgs g;
+    memset(&g, 0, sizeof g);
+    g.r = make_view(*r);
+    g.ai = make_view(*r);
+    for (int i = 0, j = 0; i < nd; ++i) {
+      if (i == axis) continue;
+      g.ai.strides[j++] = A.strides[i];
+    }
+    g.ax_len = A.dims[axis];
+    g.ax_stride = A.strides[axis];
+    g.p_stride = P.strides[0];
+    g.a = A.data;
+    g.p = P.data;
+    g.out = r->data;
+    g.n = n;
+    g.diag = diag_device();
+    if (r->dtype == HEAL_INT32)
+      axis_modsum_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    else
+      axis_modsum_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    rc = check_launch("axis_modsum");
+  }
+  scratch_free(oa);
+  scratch_free(op);
+  if (!rc) mark_written(r->data);
+  return rc;
+}
+
+// ======================================================== g_decomposition
+struct GdecArgs {
+  View a;          // input view
+  int64_t r_strides[HEAL_MAX_DIMS + 1];  // result strides (a's axes, then digit axis)
+  const void *in;
+  void *out;
+  int64_t n;
+  uint64_t power, bits;
+  int dense;       // a and result row-major
+  Diag *diag;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) gdec_kernel(const __grid_constant__ GdecArgs g) {
+  const T *A = (const T *)g.in;
+  T *R = (T *)g.out;
+  const uint64_t mask = g.bits >= 64 ? ~0ull : ((1ull << g.bits) - 1);
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ia, ir;
+    if (g.dense) {
+      ia = idx;
+      ir = idx * (int64_t)g.power;
+    } else {
+      int64_t rem = idx;
+      ia = 0;
+      ir = 0;
+      for (int i = g.a.ndim - 1; i >= 0; --i) {
+        int64_t d = g.a.dims[i];
+        int64_t c = rem % d;
+        rem /= d;
+        ia += c * g.a.strides[i];
+        ir += c * g.r_strides[i];
+      }
+    }
+    const int64_t ds = g.dense ? 1 : g.r_strides[g.a.ndim];
+    int64_t value = (int64_t)A[ia];
+    for (uint64_t d = 0; d < g.power; ++d) {
+      uint64_t uv = (uint64_t)value;
+      R[ir + (int64_t)d * ds] = (T)(int64_t)(uv & mask);
+      uint64_t q = uv >> g.bits;
+      value = sizeof(T) == 4 ? (int64_t)(int32_t)(uint32_t)q : (int64_t)q;
+    }
+    if (value > 0) {
+      unsigned long long slot = atomicAdd(&g.diag->count, 1ull);
+      if (slot < (unsigned long long)kDiagRecords) {
+        DiagRecord &rec = g.diag->rec[slot];
+        int64_t rem = idx;
+        for (int i = g.a.ndim - 1; i >= 0; --i) {
+          rec.coord[i] = rem % g.a.dims[i];
+          rem /= g.a.dims[i];
+        }
+        rec.ndim = g.a.ndim;
+        rec.kind = 1;
+        rec.base_bits = g.bits;
+        rec.power = g.power;
+      }
+    }
+  }
+}
+
+static int g_decomposition(const heal_tensor *a, const heal_tensor *r, uint64_t power, uint64_t bits) {
+  clear_error();
+  HEAL_CHECK(check_desc(a, "a", true));
+  HEAL_CHECK(check_desc(r, "result", true));
+  HEAL_CHECK(ensure_init());
+  if (a->dtype != r->dtype) return set_error(HEAL_ERR_INVALID_ARGUMENT, "all tensors must have the element type of result");
+  // g_decomposition_impl.cpp:23-26
+  bool ok = r->ndim == a->ndim + 1 && r->dims[r->ndim - 1] == (int64_t)power;
+  for (int i = 0; ok && i < a->ndim; ++i) ok = a->dims[i] == r->dims[i];
+  if (!ok) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Output must have shape a.shape + [power]");
+  if (bits >= 64) return set_error(HEAL_ERR_INVALID_ARGUMENT, "base_bits must be below 64");
+  const int64_t n = numel(*a);
+  if (n == 0) return HEAL_OK;
+  heal_tensor A = *a;
+  void *oa = nullptr;
+  int rc = HEAL_OK;
+  if (overlaps(A, *r)) rc = materialize(A, &A, &oa);
+  if (!rc) {
+    GdecArgs g;
+    memset(&g, 0, sizeof g);
+    g.a = make_view(A);
+    for (int i = 0; i < r->ndim; ++i) g.r_strides[i] = r->strides[i];
+    g.in = A.data;
+    g.out = r->data;
+    g.n = n;
+    g.power = power;
+    g.bits = bits;
+    g.dense = dense_rowmajor(A) && dense_rowmajor(*r);
+    g.diag = diag_device();
+    if (r->dtype == HEAL_INT32)
+      gdec_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    else
+      gdec_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    rc = check_launch("g_decomposition");
+  }
+  scratch_free(oa);
+  if (!rc) mark_written(r->data);
+  return rc;
+}
+
+// ================================================================ permute
+struct PermuteArgs {
+  View r, a;
+  int ew, pa;
+  int64_t m;
+  int64_t ps0, ps1;  // perms strides
+  const void *src, *perms;
+  int perms_dtype;
+  void *out;
+  int64_t n;
+  // row-major fast path: idx = (pre * m + pm) * post + inner
+  int dense;
+  int64_t post;
+  int64_t ew_div, ew_mod;  // ew coordinate = (x / ew_div) % l with x = pre or inner
+  int ew_in_post;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ PermuteArgs g) {
+  const T *A = (const T *)g.src;
+  T *R = (T *)g.out;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t src, dst;
+    if (g.dense) {
+      int64_t inner = idx % g.post;
+      int64_t rest = idx / g.post;
+      int64_t pm = rest % g.m;
+      int64_t pre = rest / g.m;
+      int64_t e = ((g.ew_in_post ? inner : pre) / g.ew_div) % g.ew_mod;
+      int64_t pidx = g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[e * g.ps0 + pm * g.ps1]
+                                                 : ((const int64_t *)g.perms)[e * g.ps0 + pm * g.ps1];
+      src = (pre * g.m + pidx) * g.post + inner;
+      dst = idx;
+    } else {
+      int64_t c[HEAL_MAX_DIMS];
+      int64_t rem = idx;
+      for (int i = g.r.ndim - 1; i >= 0; --i) {
+        c[i] = rem % g.r.dims[i];
+        rem /= g.r.dims[i];
+      }
+      int64_t e = c[g.ew], pm = c[g.pa];
+      int64_t pidx = g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[e * g.ps0 + pm * g.ps1]
+                                                 : ((const int64_t *)g.perms)[e * g.ps0 + pm * g.ps1];
+      c[g.pa] = pidx;
+      src = 0;
+      dst = 0;
+      for (int i = 0; i < g.r.ndim; ++i) {
+        src += c[i] * g.a.strides[i];
+        dst += (i == g.pa ? pm : c[i]) * g.r.strides[i];
+      }
+    }
+    R[dst] = A[src];
+  }
+}
+
+static int permute(const heal_tensor *a, const heal_tensor *perms, const heal_tensor *r, int64_t ew, int64_t pa) {
+  clear_error();
+  HEAL_CHECK(check_desc(a, "a", true));
+  HEAL_CHECK(check_desc(perms, "perms", true));
+  HEAL_CHECK(check_desc(r, "result", true));
+  HEAL_CHECK(ensure_init());
+  if (a->dtype != r->dtype) return set_error(HEAL_ERR_INVALID_ARGUMENT, "all tensors must have the element type of result");
+  // permute_impl.cpp:19-35
+  const int nd = a->ndim;
+  if (!same_dims(*a, *r)) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Result shape must match input shape.");
+  if (ew < 0 || ew >= nd || pa < 0 || pa >= nd) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Axis out of bounds.");
+  if (ew == pa) return set_error(HEAL_ERR_INVALID_ARGUMENT, "elementwise_axis and perm_axis must be different.");
+  const int64_t l = a->dims[ew], m = a->dims[pa];
+  if (perms->ndim != 2 || perms->dims[0] != l || perms->dims[1] != m)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT,
+                     "Perms must have shape [l, m] where l and m match a.shape at elementwise and perm axes.");
+  const int64_t n = numel(*a);
+  if (n == 0) return HEAL_OK;
+  bool valid = false;
+  HEAL_CHECK(perms_valid(*perms, m, &valid));
+  if (!valid) return set_error(HEAL_ERR_OUT_OF_RANGE, "Permutation index out of bounds.");
+  heal_tensor A = *a, PR = *perms;
+  void *oa = nullptr, *op = nullptr;
+  int rc = HEAL_OK;
+  if (overlaps(A, *r)) rc = materialize(A, &A, &oa);
+  if (!rc && overlaps(PR, *r)) rc = materialize(PR, &PR, &op);
+  if (!rc) {
+    PermuteArgs g;
+    memset(&g, 0, sizeof g);
+    g.r = make_view(*r);
+    g.a = make_view(A);
+    g.ew = (int)ew;
+    g.pa = (int)pa;
+    g.m = m;
+    g.ps0 = PR.strides[0];
+    g.ps1 = PR.strides[1];
+    g.src = A.data;
+    g.perms = PR.data;
+    g.perms_dtype = PR.dtype;
+    g.out = r->data;
+    g.n = n;
+    g.dense = dense_rowmajor(A) && dense_rowmajor(*r);
+    if (g.dense) {
+      int64_t post = 1;
+      for (int i = (int)pa + 1; i < nd; ++i) post *= a->dims[i];
+      g.post = post;
+      g.ew_in_post = ew > pa;
+      int64_t div = 1;
+      if (ew > pa) {
+        for (int i = (int)ew + 1; i < nd; ++i) div *= a->dims[i];
+      } else {
+        for (int i = (int)ew + 1; i < (int)pa; ++i) div *= a->dims[i];
+      }
+      g.ew_div = div;
+      g.ew_mod = l;
+    }
+    if (r->dtype == HEAL_INT32)
+      permute_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    else
+      permute_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    rc = check_launch("permute");
+  }
+  scratch_free(oa);
+  scratch_free(op);
+  if (!rc) mark_written(r->data);
+  return rc;
+}
+
+}  // namespace heal
+
+using namespace heal;
+
+extern "C" {
+
+int heal_axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_tensor *result, int64_t axis) {
+  return axis_modsum(a, p, result, axis);
+}
+
+int heal_g_decomposition(const heal_tensor *a, const heal_tensor *result, uint64_t power, uint64_t base_bits) {
+  return g_decomposition(a, result, power, base_bits);
+}
+
+int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tensor *result, int64_t elementwise_axis,
+                 int64_t perm_axis) {
+  return permute(a, perms, result, elementwise_axis, perm_axis);
+}
+
+}  // extern "C"

@@ -117,7 +117,7 @@ def modsum(a, b, p, out_shape=None):
 
 def modneg(a, p, out_shape=None):
     """Extension: (p - a % p) % p in the double-width type."""
-    return _modop(2, a, None, p, out_shape or a.shape, a.dtype)
+    return _modop(2, a, 0, p, out_shape or a.shape, a.dtype)
 
 
 def mod(a, b, dtype=None, shape=None):

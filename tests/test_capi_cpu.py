@@ -1,0 +1,98 @@
+"""CPU-only checks of the C ABI: the library loads and exports every symbol
+include/heal_gb300.h declares, the `lattica_hw` module exposes HEAL's names,
+and the stride-only metadata edits follow DeviceTensor::reshape and the
+virtual ops of example_impl (no device memory is touched)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import heal_gb300
+from heal_gb300 import capi
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    heal_gb300.build()
+
+
+def test_exports_every_declared_symbol():
+    names = capi.declared_symbols()
+    assert len(names) >= 40
+    L = ctypes.CDLL(capi.LIB_PATH)
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(names) == set(capi.SIGNATURES), set(names) ^ set(capi.SIGNATURES)
+
+
+def test_lattica_hw_module_names():
+    m = heal_gb300.lattica_hw()
+    # every name HEAL's example_impl/py_bindings.cpp:87-133 binds
+    names = ["DeviceTensor32", "DeviceTensor64", "DeviceTensorfloat64", "axis_modsum_32", "axis_modsum_64",
+             "ntt_32", "ntt_64", "intt_32", "intt_64", "permute_32", "permute_64"]
+    for sfx in ("32", "64", "float64"):
+        names += [f"{n}_{sfx}" for n in ("allocate_on_hardware", "host_to_device", "device_to_host", "expand",
+                                          "squeeze", "unsqueeze", "make_contiguous")]
+    for sfx in ("32", "64"):
+        names += [f"{op}_{v}_{sfx}" for op in ("modmul", "modsum") for v in ("ttt", "ttc", "tct", "tcc")]
+        names += [f"g_decomposition_{sfx}"]
+    missing = [n for n in names if not hasattr(m, n)]
+    assert not missing, missing
+    for cls in ("DeviceTensor32", "DeviceTensor64", "DeviceTensorfloat64"):
+        for meth in ("print", "print_metadata", "reshape"):
+            assert hasattr(getattr(m, cls), meth)
+
+
+def t(shape, strides=None, dtype=np.int64):
+    st = strides or capi._rowmajor(shape)
+    return capi.desc(None, dtype, shape, st)
+
+
+def dims(d):
+    return list(d.dims)[:d.ndim], list(d.strides)[:d.ndim]
+
+
+def test_reshape_rules():
+    L = capi.lib()
+    d = t((2, 2, 3))
+    nd = (ctypes.c_int64 * 2)(6, 2)
+    assert L.heal_tensor_reshape(ctypes.byref(d), 2, nd) == 0
+    assert dims(d) == ([6, 2], [2, 1])
+    bad = (ctypes.c_int64 * 2)(5, 2)
+    assert L.heal_tensor_reshape(ctypes.byref(d), 2, bad) == 1
+    assert b"Total size of new shape" in L.heal_last_error()
+    # a broadcast (stride-0) axis does not count (device_memory_impl.cpp:45-50)
+    e = t((3, 4), (0, 1))
+    four = (ctypes.c_int64 * 1)(4)
+    assert L.heal_tensor_reshape(ctypes.byref(e), 1, four) == 0
+    assert dims(e) == ([4], [1])
+
+
+def test_virtual_ops():
+    L = capi.lib()
+    d = t((1, 1, 3))
+    assert L.heal_tensor_squeeze(ctypes.byref(d), 1) == 0 and dims(d) == ([1, 3], [3, 1])
+    assert L.heal_tensor_squeeze(ctypes.byref(d), 1) == 1   # size 3: invalid_argument
+    d = t((2, 2))
+    assert L.heal_tensor_unsqueeze(ctypes.byref(d), -1) == 0 and dims(d) == ([2, 2, 1], [2, 1, 0])
+    d = t((2, 3))
+    assert L.heal_tensor_unsqueeze(ctypes.byref(d), 4) == 1
+    assert L.heal_tensor_unsqueeze(ctypes.byref(d), -4) == 1
+    d = t((2, 1))
+    assert L.heal_tensor_expand(ctypes.byref(d), 1, 3) == 0 and dims(d) == ([2, 3], [1, 0])
+    assert L.heal_tensor_expand(ctypes.byref(d), 1, 3) == 1  # not size 1
+    assert L.heal_tensor_expand(ctypes.byref(d), 0, 0) == 1  # repeats <= 0
+    d = t((2, 3, 4))
+    assert L.heal_tensor_moveaxis(ctypes.byref(d), 2, 0) == 0 and dims(d) == ([4, 2, 3], [1, 12, 4])
+    d = t((5, 6))
+    assert L.heal_tensor_slice(ctypes.byref(d), 1, 1, 5, 2) == 0 and dims(d) == ([5, 2], [6, 2])
+
+
+def test_contiguity_and_span():
+    L = capi.lib()
+    assert L.heal_tensor_is_contiguous(ctypes.byref(t((3, 4)))) == 1
+    assert L.heal_tensor_is_contiguous(ctypes.byref(t((4, 3), (1, 4)))) == 0
+    assert L.heal_tensor_is_contiguous(ctypes.byref(t((3, 1, 4), (4, 99, 1)))) == 1  # size-1 axes skipped
+    assert L.heal_tensor_span(ctypes.byref(t((4, 3), (1, 4)))) == 12
+    assert L.heal_tensor_span(ctypes.byref(t((3, 4), (0, 1)))) == 4
+    assert L.heal_tensor_span(ctypes.byref(t((0, 4)))) == 0

@@ -1,0 +1,293 @@
+"""Bit-exact parity of the GPU backend with HEAL's sample implementation,
+through the C ABI: every golden array the reference itself produced
+(tests/golden/), and the CPU oracle on seeded inputs across sizes, element
+types, modulus widths, strides and permutations."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from heal_gb300 import capi
+from heal_gb300 import params as P
+from oracle import oracle as O
+from _gpu import intt, ntt, ready, run, up
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def gpu():
+    return ready()
+
+
+def sha(x):
+    return hashlib.sha256(np.ascontiguousarray(x).tobytes()).hexdigest()
+
+
+# ============================================================ golden vectors
+def test_ntt_pin(golden):
+    g = golden("ntt_pin")
+    fw = ntt(g["a"], g["p"], g["perm"], g["tw"])
+    assert np.array_equal(fw, g["ntt"])
+    assert np.array_equal(intt(fw, g["p"], g["perm"], g["itw"], g["minv"]), g["a"])
+
+
+@pytest.mark.parametrize("case", ["ntt_i64", "ntt_i64_m1", "ntt_i64_m2", "ntt_i64_m4096", "ntt_i32", "ntt_neg"])
+def test_ntt_golden(golden, case):
+    g = golden(case)
+    assert np.array_equal(ntt(g["a"], g["p"], g["perm"], g["tw"]), g["ntt"])
+    src = g["ntt"] if "intt_a" in g else g["a"]
+    got = intt(src, g["p"], g["perm"], g["itw"], g["minv"])
+    assert np.array_equal(got, O.intt(src, g["p"], g["perm"], g["itw"], g["minv"], exact=1))
+    width = 31 if g["a"].dtype == np.int32 else 63
+    if int(g["p"].max()) ** 2 < 2 ** width:   # where the reference's m_inv product cannot wrap
+        assert np.array_equal(got, g["intt"])
+    if "intt_a" in g:
+        assert np.array_equal(got, g["a"])
+
+
+def test_ntt_negative_twiddles(golden):
+    g = golden("ntt_negtw")
+    assert np.array_equal(ntt(g["a"], g["p"], g["perm"], g["tw"]), g["ntt"])
+
+
+def test_ntt_general_and_duplicate_perm(golden):
+    g = golden("ntt_perm")
+    assert np.array_equal(ntt(g["a"], g["p"], g["perm"], g["tw"]), g["ntt"])
+    assert np.array_equal(intt(g["a"], g["p"], g["perm"], g["itw"], g["minv"]), g["intt"])
+    assert np.array_equal(ntt(g["a"], g["p"], g["dup"], g["tw"]), g["ntt_dup"])
+    assert np.array_equal(intt(g["a"], g["p"], g["dup"], g["itw"], g["minv"]), g["intt_dup"])
+
+
+def test_cfg2_shaped_chain_golden(golden):
+    g = golden("cfg2_small")
+    p, perm, tw = g["p"], g["perm"], g["tw"]
+    assert np.array_equal(ntt(g["ct"], p, perm, tw), g["ntt_ct"])
+    x = intt(g["ct"], p, perm, g["itw"], g["minv"])
+    assert np.array_equal(x, O.intt(g["ct"], p, perm, g["itw"], g["minv"], exact=1))
+    dig = run("heal_g_decomposition", g["coef"], 3, 17, out_shape=g["digits"].shape, dtype=np.int64)
+    assert np.array_equal(dig, g["digits"])
+    L = len(p)
+    p_t = np.repeat(p, 3)
+    dn = ntt(g["digits"].reshape(2, -1, 1, L * 3), p_t, perm, np.repeat(tw, 3, axis=0))
+    assert np.array_equal(dn, g["dn"])
+    prod = run("heal_modmul_ttt", g["dn"], g["key"], p_t, out_shape=g["dn"].shape, dtype=np.int64)
+    assert np.array_equal(prod, g["prod"])
+    moved = up(g["prod"]).reshape((2, g["prod"].shape[1], 1, L, 3)).moveaxis(4, 3)
+    acc = run("heal_axis_modsum", moved, p, 3, out_shape=g["acc"].shape, dtype=np.int64)
+    assert np.array_equal(acc, g["acc"])
+    rot = run("heal_permute", g["acc"], g["gal"], 2, 1, out_shape=g["acc"].shape, dtype=np.int64)
+    assert np.array_equal(rot, g["rot"])
+
+
+@pytest.mark.parametrize("tag,dt", [("32", np.int32), ("64", np.int64)])
+@pytest.mark.parametrize("op", ["modmul", "modsum"])
+def test_modops_golden(golden, tag, dt, op):
+    g = golden(f"{op}_{tag}")
+    f = f"heal_{op}"
+    assert np.array_equal(run(f + "_ttt", g["a"], g["b"], g["p"], out_shape=g["a"].shape, dtype=dt), g["ttt"])
+    assert np.array_equal(run(f + "_ttt", g["an"], g["bn"], g["pn"], out_shape=g["an"].shape, dtype=dt), g["ttt_neg"])
+    assert np.array_equal(run(f + "_ttt", g["at"], g["at"], g["p"], out_shape=g["at"].shape, dtype=dt),
+                          g["ttt_strided"])
+    assert np.array_equal(run(f + "_ttt", g["col"], g["row"], g["prow"], out_shape=(2, 3), dtype=dt), g["ttt_bcast"])
+    assert np.array_equal(run(f + "_ttc", g["an"], g["bn"], 1000003, out_shape=g["an"].shape, dtype=dt), g["ttc"])
+    assert np.array_equal(run(f + "_tct", g["an"], -12345, g["pn"], out_shape=g["an"].shape, dtype=dt), g["tct"])
+    assert np.array_equal(run(f + "_tcc", g["an"], 98765, 4099, out_shape=g["an"].shape, dtype=dt), g["tcc"])
+
+
+@pytest.mark.parametrize("tag", ["32", "64"])
+def test_axis_modsum_golden(golden, tag):
+    g = golden(f"axis_modsum_{tag}")
+    a = g["a"]
+    for ax in (0, 1, 2):
+        shape = tuple(d for i, d in enumerate(a.shape) if i != ax)
+        assert np.array_equal(run("heal_axis_modsum", a, g["p"], ax, out_shape=shape, dtype=a.dtype), g[f"ax{ax}"])
+    seq = run("heal_axis_modsum", np.array([[5], [5], [-8]], a.dtype), np.array([7], a.dtype), 0,
+              out_shape=(1,), dtype=a.dtype)
+    assert np.array_equal(seq, g["seq"])
+
+
+@pytest.mark.parametrize("tag", ["32", "64"])
+def test_g_decomposition_golden(golden, tag):
+    g = golden(f"gdec_{tag}")
+    a = g["a"]
+    for key, (pw, bits) in {"b3p4": (4, 3), "b17p3": (3, 17), "b1p40": (40, 1)}.items():
+        got = run("heal_g_decomposition", a, pw, bits, out_shape=a.shape + (pw,), dtype=a.dtype)
+        assert np.array_equal(got, g[key]), key
+    capi.synchronize()
+
+
+@pytest.mark.parametrize("tag", ["32", "64"])
+def test_permute_golden(golden, tag):
+    g = golden(f"permute_{tag}")
+    a = g["a"]
+    assert np.array_equal(run("heal_permute", a, g["perms_a"], 1, 2, out_shape=a.shape, dtype=a.dtype), g["r12"])
+    assert np.array_equal(run("heal_permute", a, g["perms_b"], 0, 3, out_shape=a.shape, dtype=a.dtype), g["r03"])
+
+
+def test_cfg1_full_size_hashes(golden_hash):
+    # [8, 4096, 1, 4] int64 with the four largest 30-bit NTT primes, checked
+    # against the reference's own outputs by SHA-256
+    h = golden_hash["cfg1"]
+    qs = P.ntt_primes(h["bound"], h["N"], h["L"])
+    p, perm, tw, itw, minv = P.ntt_tables(qs, h["N"])
+    A = P.residues(h["seeds"][0], h["shape"], qs)
+    B = P.residues(h["seeds"][1], h["shape"], qs)
+    NA, NB = ntt(A, p, perm, tw), ntt(B, p, perm, tw)
+    assert sha(NA) == h["ntt_a"] and sha(NB) == h["ntt_b"]
+    assert sha(intt(NA, p, perm, itw, minv)) == h["intt_ntt_a"]
+    PR = run("heal_modmul_ttt", NA, NB, p, out_shape=NA.shape, dtype=np.int64)
+    assert sha(PR) == h["modmul"]
+    AS = run("heal_axis_modsum", PR, p, 0, out_shape=PR.shape[1:], dtype=np.int64)
+    assert sha(AS) == h["axis_modsum"]
+
+
+def test_n65536_hash(golden_hash):
+    h = golden_hash["n65536_i64"]
+    qs = P.ntt_primes(h["bound"], h["N"], h["L"])
+    p, perm, tw, itw, minv = P.ntt_tables(qs, h["N"])
+    X = P.residues(h["seed"], h["shape"], qs)
+    fw = ntt(X, p, perm, tw)
+    assert sha(fw) == h["ntt"]
+    assert np.array_equal(intt(fw, p, perm, itw, minv), X)
+
+
+# ============================================================ oracle sweeps
+NTT_CASES = [
+    # (shape [l, m, r, k], dtype, prime bound)
+    ((3, 2, 1, 2), np.int64, 2**30),
+    ((2, 8, 2, 3), np.int64, 2**50),
+    ((1, 64, 1, 5), np.int32, 2**30),
+    ((2, 256, 3, 8), np.int64, 2**62),
+    ((1, 1024, 1, 9), np.int32, 2**31),
+    ((2, 2048, 1, 4), np.int64, 2**40),
+    ((1, 8192, 1, 3), np.int64, 2**50),   # two passes (64 x 128)
+    ((2, 8192, 1, 2), np.int32, 2**30),
+    ((1, 16384, 2, 3), np.int64, 2**31),
+]
+
+
+@pytest.mark.parametrize("shape,dt,bound", NTT_CASES)
+def test_ntt_intt_vs_oracle(shape, dt, bound):
+    l, m, r, k = shape
+    qs = P.ntt_primes(bound, max(m, 2), k)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m, dt)
+    a = P.residues(hash(shape) & 0xFFFF, shape, qs, dt)
+    fw = ntt(a, p, perm, tw)
+    assert np.array_equal(fw, O.ntt(a, p, perm, tw))
+    back = intt(fw, p, perm, itw, minv)
+    assert np.array_equal(back, a)
+    assert np.array_equal(intt(a, p, perm, itw, minv), O.intt(a, p, perm, itw, minv, exact=1))
+
+
+@pytest.mark.parametrize("m", [8192, 65536])
+def test_two_pass_general_and_duplicate_perm(m):
+    qs = P.ntt_primes(2**40, m, 2)
+    p, _, tw, itw, minv = P.ntt_tables(qs, m)
+    perm = np.argsort(P.splitmix64(m, m)).astype(np.int64)
+    a = P.residues(5, (1, m, 1, 2), qs)
+    assert np.array_equal(ntt(a, p, perm, tw), O.ntt(a, p, perm, tw))
+    assert np.array_equal(intt(a, p, perm, itw, minv), O.intt(a, p, perm, itw, minv))
+    dup = perm.copy()
+    dup[5] = dup[11]
+    prior = P.residues(6, (1, m, 1, 2), qs)
+    assert np.array_equal(ntt(a, p, dup, tw), O.ntt(a, p, dup, tw))
+    assert np.array_equal(intt(a, p, dup, itw, minv, prior=prior),
+                          O.intt(a, p, dup, itw, minv, result=prior))
+
+
+@pytest.mark.parametrize("m", [64, 8192])
+def test_ntt_non_canonical_inputs(m):
+    # values >= q and negative values take the reference's own arithmetic
+    qs = P.ntt_primes(2**30, m, 2)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m)
+    a = P.uniform(9, (1, m, 1, 2), -(2**40), 2**40)
+    b = P.uniform(10, (1, m, 1, 2), 0, 2**40)
+    for x in (a, b):
+        assert np.array_equal(ntt(x, p, perm, tw), O.ntt(x, p, perm, tw))
+        assert np.array_equal(intt(x, p, perm, itw, minv), O.intt(x, p, perm, itw, minv))
+
+
+def test_ntt_strided_input_and_in_place():
+    m, k = 4096, 6
+    qs = P.ntt_primes(2**50, m, k)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m)
+    limb_major = np.ascontiguousarray(np.moveaxis(P.residues(11, (2, m, k), qs), 2, 1))  # [2, k, m]
+    view = np.moveaxis(limb_major, 1, 2)[:, :, None, :]                                 # [2, m, 1, k]
+    assert not view.flags.c_contiguous
+    want = O.ntt(np.ascontiguousarray(view), p, perm, tw)
+    assert np.array_equal(ntt(view, p, perm, tw), want)
+    # in place: result aliases a
+    d = up(np.ascontiguousarray(view))
+    capi.call("heal_ntt", d, up(p), up(perm), up(tw), None, None, d)
+    assert np.array_equal(d.numpy(), want)
+    capi.call("heal_intt", d, up(p), up(perm), up(itw), up(minv), None, None, d)
+    assert np.array_equal(d.numpy(), view)
+
+
+def test_ntt_errors():
+    qs = P.ntt_primes(2**30, 8, 2)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, 8)
+    a = P.residues(1, (1, 8, 1, 2), qs)
+    with pytest.raises(ValueError):
+        ntt(a.reshape(8, 2), p, perm, tw)
+    with pytest.raises(ValueError):
+        ntt(a, p[:1], perm, tw)
+    with pytest.raises(ValueError):
+        ntt(a, p, perm[:4], tw)
+    with pytest.raises(ValueError):
+        ntt(a, p, perm, tw[:, :4])
+    bad = perm.copy()
+    bad[3] = 8
+    with pytest.raises(IndexError):
+        ntt(a, p, bad, tw)
+    with pytest.raises(IndexError):
+        intt(a, p, perm, itw, minv[:1])
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+def test_modops_vs_oracle_random(dt):
+    big = 2**31 if dt == np.int32 else 2**63
+    shape = (3, 5, 7, 16)
+    qs = np.array(P.ntt_primes(2**30 if dt == np.int32 else 2**62, 8, 16), dt)
+    a = P.uniform(1, shape, 0, int(qs.min()), dt)
+    b = P.uniform(2, shape, 0, int(qs.min()), dt)
+    for f, o in [("heal_modmul_ttt", O.modmul), ("heal_modsum_ttt", O.modsum)]:
+        assert np.array_equal(run(f, a, b, qs, out_shape=shape, dtype=dt), o(a, b, qs))
+    an = P.uniform(3, shape, -big // 2, big // 2, dt)
+    bn = P.uniform(4, (7, 1), -big // 2, big // 2, dt)
+    for f, o in [("heal_modmul_ttt", O.modmul), ("heal_modsum_ttt", O.modsum)]:
+        assert np.array_equal(run(f, an, bn, qs, out_shape=shape, dtype=dt), o(an, bn, qs, out_shape=shape))
+    assert np.array_equal(run("heal_modneg_tt", an, qs, out_shape=shape, dtype=dt), O.modneg(an, qs))
+    assert np.array_equal(run("heal_modneg_tc", a, 65537, out_shape=shape, dtype=dt), O.modneg(a, 65537))
+    den = P.uniform(14, shape, -1000, 1000, dt)
+    den[den == 0] = 3
+    assert np.array_equal(run("heal_mod_tt", an, den, out_shape=shape, dtype=dt), O.mod(an, den))
+    assert np.array_equal(run("heal_mod_tc", an, 97, out_shape=shape, dtype=dt), O.mod(an, 97))
+    # odd sizes: a tail that is not a multiple of the 16-byte vector
+    odd = P.uniform(5, (3, 7), 0, 1000, dt)
+    assert np.array_equal(run("heal_modmul_ttc", odd, odd, 997, out_shape=odd.shape, dtype=dt),
+                          O.modmul(odd, odd, 997))
+
+
+def test_zero_size_and_aliasing():
+    z = np.zeros((0, 4), np.int64)
+    assert run("heal_modmul_ttt", z, z, np.array([7, 7, 7, 7]), out_shape=(0, 4), dtype=np.int64).shape == (0, 4)
+    # result overlapping an input in another layout
+    x = P.uniform(7, (4, 4), 0, 100)
+    d = up(x)
+    t = capi.DeviceArray(d.buf, np.int64, (4, 4), (1, 4))   # transposed view of the same buffer
+    capi.call("heal_modsum_tcc", t, 1, 1000, d)
+    assert np.array_equal(d.numpy(), (x.T + 1) % 1000)
+
+
+def test_permute_and_axis_modsum_vs_oracle():
+    for dt in (np.int32, np.int64):
+        a = P.uniform(12, (2, 1024, 1, 24), 0, 2**30, dt)
+        gal = P.galois_perm(1024, 5).reshape(1, 1024).astype(dt)
+        assert np.array_equal(run("heal_permute", a, gal, 2, 1, out_shape=a.shape, dtype=dt), O.permute(a, gal, 2, 1))
+        moved = np.moveaxis(P.uniform(13, (2, 64, 1, 5, 3), -2**20, 2**30, dt), 4, 3)
+        p = np.array(P.ntt_primes(2**30, 8, 5), dt)
+        got = run("heal_axis_modsum", up(np.ascontiguousarray(np.moveaxis(moved, 3, 4))).moveaxis(4, 3), p, 3,
+                  out_shape=(2, 64, 1, 5), dtype=dt)
+        assert np.array_equal(got, O.axis_modsum(moved, p, 3))
