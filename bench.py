@@ -299,6 +299,41 @@ def our_arm(args):
     return 0
 
 
+def ntt_probe(args):
+    """--mode ntt: the batched NTT alone on [batch, 65536, 1, 72] int64 (the
+    digit tensor of `batch` / 2 chains); used for ncu captures of the pass
+    kernels.  Prints one JSON line with the CUDA-event time per call."""
+    import torch
+    import heal_gb300
+    from heal_gb300 import capi
+    from heal_gb300 import params as P
+    heal_gb300.build()
+    capi.check(capi.lib().heal_init(0))
+    stream = torch.cuda.ExternalStream(capi.stream())
+    qs = P.ntt_primes(1 << BOUND, N, L)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, N)
+    p_t, tw_t = np.repeat(p, D), np.repeat(tw, D, axis=0)
+    shape = (args.batch, N, 1, L * D)
+    x = capi.DeviceArray.from_numpy(P.residues(3, shape, p_t))
+    y = capi.DeviceArray.empty(shape, np.int64)
+    dev = [capi.DeviceArray.from_numpy(v) for v in (p_t, perm, tw_t)]
+    call = lambda: capi.call("heal_ntt", x, dev[0], dev[1], dev[2], None, None, y)
+    for _ in range(args.warmup):
+        call()
+    capi.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        call()
+    stop.record(stream)
+    stop.synchronize()
+    ms = start.elapsed_time(stop) / args.steps
+    limbs = args.batch * L * D
+    print(json.dumps({"mode": "ntt", "shape": list(shape), "ms_per_call": ms, "limbs_per_s": limbs / (ms / 1e3),
+                      "algorithmic_GBps": 2 * limbs * N * 8 / (ms / 1e3) / 1e9}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -307,9 +342,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--mode", default="chain", choices=["chain", "ntt"])
+    ap.add_argument("--batch", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.mode == "ntt":
+        return ntt_probe(args)
     if args.impl == "reference":
         return reference_arm(args)
     return our_arm(args)

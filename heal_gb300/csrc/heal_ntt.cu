@@ -34,240 +34,16 @@
 #include <string>
 
 #include "heal_internal.h"
+#include "heal_ntt_kernels.cuh"
 
 namespace heal {
 
-enum { KIND_STRIDED = 0, KIND_BLOCK = 1 };
-constexpr int kNttThreads = 256;
 constexpr int kSinglePassLogMax = 12;  // m <= 4096 in one pass
 
-struct NttArgs {
-  const void *src;
-  int64_t ss[4];
-  const void *old;  // INTT: previous result contents for rows no index maps to
-  int64_t os[4];
-  void *dst;
-  int64_t ds[4];
-  int64_t l, m, r, k;
-  int p, logC, C;
-  int kind;
-  int64_t nsets;     // sets (strided) or blocks per column
-  int64_t ngroups_t; // ceil(k / C)
-  const int32_t *load_map;
-  const int32_t *store_gather;
-  const int32_t *store_scatter;
-  const void *tw_pairs;
-  const int *tw_neg;
-  const void *tw_raw;
-  int64_t tw_s0, tw_s1;
-  const int64_t *q;
-  const void *minv_pairs;
-  const int *minv_neg;
-  const void *minv_raw;
-  int64_t minv_s0;
-  int scale;
-  int canon_load;
-  int force_exact;
-};
-
-template <bool WIDE>
-struct Word;
-template <>
-struct Word<true> {
-  typedef uint64_t W;
-  typedef ulonglong2 Pair;
-};
-template <>
-struct Word<false> {
-  typedef uint32_t W;
-  typedef uint2 Pair;
-};
-
-template <bool WIDE>
-__device__ __forceinline__ typename Word<WIDE>::W mulw(typename Word<WIDE>::W y, typename Word<WIDE>::Pair pr,
-                                                        typename Word<WIDE>::W q) {
-  if (WIDE)
-    return (typename Word<WIDE>::W)shoup64((uint64_t)y, (uint64_t)pr.x, (uint64_t)pr.y, (uint64_t)q);
-  return (typename Word<WIDE>::W)shoup32((uint32_t)y, (uint32_t)pr.x, (uint32_t)pr.y, (uint32_t)q);
-}
-
-template <typename T>
-__device__ __forceinline__ int64_t ld_raw(const void *base, int64_t off) {
-  return (int64_t)((const T *)base)[off];
-}
-
-__device__ __forceinline__ int64_t raw_any(const void *base, int64_t off, bool is32) {
-  return is32 ? (int64_t)((const int32_t *)base)[off] : ((const int64_t *)base)[off];
-}
-
-template <typename T, bool WIDE, bool INV>
-__global__ void __launch_bounds__(kNttThreads) ntt_pass_kernel(const __grid_constant__ NttArgs g) {
-  typedef typename Word<WIDE>::W W;
-  typedef typename Word<WIDE>::Pair Pair;
-  extern __shared__ __align__(16) int64_t tile[];
-
-  const int P = 1 << g.p;
-  const int C = g.C, logC = g.logC;
-  const int64_t bid = blockIdx.x;
-  const int64_t rset = bid % g.nsets;
-  const int64_t cg = bid / g.nsets;
-  const int64_t tg = cg % g.ngroups_t;
-  const int64_t ij = cg / g.ngroups_t;
-  const int64_t j = ij % g.r, i = ij / g.r;
-  const int64_t t0 = tg * C;
-  const bool is32 = sizeof(T) == 4;
-
-  auto row_of = [&](int64_t s) -> int64_t {
-    return g.kind == KIND_BLOCK ? rset * P + s : rset + s * g.nsets;
-  };
-
-  // ---- load the tile (raw values)
-  int neg = 0;
-  const int64_t sb = i * g.ss[0] + j * g.ss[2];
-  for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
-    const int s = e >> logC, c = e & (C - 1);
-    const int64_t t = t0 + c;
-    if (t >= g.k) continue;
-    const int64_t v = row_of(s);
-    int64_t x;
-    if (g.load_map) {
-      const int32_t sr = g.load_map[v];
-      if (sr < 0)
-        x = ld_raw<T>(g.old, i * g.os[0] + v * g.os[1] + j * g.os[2] + t * g.os[3]);
-      else
-        x = ld_raw<T>(g.src, sb + (int64_t)sr * g.ss[1] + t * g.ss[3]);
-    } else {
-      x = ld_raw<T>(g.src, sb + v * g.ss[1] + t * g.ss[3]);
-    }
-    // Negative values always need the reference's arithmetic.  For the
-    // inverse so do values >= q: its first butterfly forms u + q - v, which
-    // goes negative when v > u + q.  The forward NTT reduces them instead
-    // (its stage-1 outputs are canonical whenever the inputs are >= 0).
-    neg |= x < 0 || (INV && g.canon_load && x >= g.q[t]);
-    tile[e] = x;
-  }
-  bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
-               (g.scale && g.minv_neg && *g.minv_neg);
-
-  const int64_t G = g.kind == KIND_BLOCK ? g.nsets + rset : 1;
-  const int nbf = (P >> 1) * C;
-
-  if (!exact) {
-    // ---- fast path: canonical residues, Shoup butterflies
-    if (g.canon_load) {
-      for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
-        const int64_t t = t0 + (e & (C - 1));
-        if (t >= g.k) continue;
-        const uint64_t q = (uint64_t)g.q[t];
-        const uint64_t x = (uint64_t)tile[e];
-        if (x >= q) tile[e] = (int64_t)(x % q);
-      }
-      __syncthreads();
-    }
-    for (int st = 0; st < g.p; ++st) {
-      for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
-        const int c = b & (C - 1);
-        const int64_t t = t0 + c;
-        if (t >= g.k) continue;
-        const int jb = b >> logC;
-        int su, sv;
-        int64_t twidx;
-        if (!INV) {
-          const int hl = g.p - 1 - st;  // log2 of the pair distance
-          const int grp = jb >> hl;
-          su = (grp << (hl + 1)) + (jb & ((1 << hl) - 1));
-          sv = su + (1 << hl);
-          twidx = (G << st) + grp;
-        } else {
-          const int grp = jb >> st;
-          su = (grp << (st + 1)) + (jb & ((1 << st) - 1));
-          sv = su + (1 << st);
-          twidx = G * (int64_t)(P >> (st + 1)) + grp;
-        }
-        const W q = (W)g.q[t];
-        const Pair pr = __ldg((const Pair *)g.tw_pairs + t * g.m + twidx);
-        const W u = (W)tile[(su << logC) + c];
-        const W v = (W)tile[(sv << logC) + c];
-        W nu, nv;
-        if (!INV) {
-          const W tv = mulw<WIDE>(v, pr, q);
-          nu = u + tv;
-          nu = nu >= q ? nu - q : nu;
-          nv = u >= tv ? u - tv : u + (q - tv);
-        } else {
-          nu = u + v;
-          nu = nu >= q ? nu - q : nu;
-          const W d = u >= v ? u - v : u + (q - v);
-          nv = mulw<WIDE>(d, pr, q);
-        }
-        tile[(su << logC) + c] = (int64_t)nu;
-        tile[(sv << logC) + c] = (int64_t)nv;
-      }
-      __syncthreads();
-    }
-  } else {
-    // ---- exact path: the reference's arithmetic, C's `%` in __int128
-    for (int st = 0; st < g.p; ++st) {
-      for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
-        const int c = b & (C - 1);
-        const int64_t t = t0 + c;
-        if (t >= g.k) continue;
-        const int jb = b >> logC;
-        int su, sv;
-        int64_t twidx;
-        if (!INV) {
-          const int hl = g.p - 1 - st;
-          const int grp = jb >> hl;
-          su = (grp << (hl + 1)) + (jb & ((1 << hl) - 1));
-          sv = su + (1 << hl);
-          twidx = (G << st) + grp;
-        } else {
-          const int grp = jb >> st;
-          su = (grp << (st + 1)) + (jb & ((1 << st) - 1));
-          sv = su + (1 << st);
-          twidx = G * (int64_t)(P >> (st + 1)) + grp;
-        }
-        const int64_t q = g.q[t];
-        const int64_t s = raw_any(g.tw_raw, t * g.tw_s0 + twidx * g.tw_s1, is32);
-        const int64_t u = tile[(su << logC) + c];
-        const int64_t v = tile[(sv << logC) + c];
-        int64_t nu, nv;
-        if (!INV) {
-          const int64_t vm = crem128((i128)v * s, q);
-          nu = crem128((i128)u + vm, q);
-          nv = crem128((i128)u + q - vm, q);
-        } else {
-          nu = crem128((i128)u + v, q);
-          nv = crem128(((i128)u + q - v) * s, q);
-        }
-        tile[(su << logC) + c] = nu;
-        tile[(sv << logC) + c] = nv;
-      }
-      __syncthreads();
-    }
-  }
-
-  // ---- store
-  const int64_t db = i * g.ds[0] + j * g.ds[2];
-  for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
-    const int s = e >> logC, c = e & (C - 1);
-    const int64_t t = t0 + c;
-    if (t >= g.k) continue;
-    int64_t x = g.store_gather ? tile[((int)g.store_gather[s] << logC) + c] : tile[e];
-    if (g.scale) {
-      const int64_t q = g.q[t];
-      if (!exact) {
-        const Pair pr = __ldg((const Pair *)g.minv_pairs + t);
-        x = (int64_t)mulw<WIDE>((W)x, pr, (W)q);
-      } else {
-        x = crem128((i128)x * raw_any(g.minv_raw, t * g.minv_s0, is32), q);
-      }
-    }
-    const int64_t v = row_of(s);
-    const int64_t dr = g.store_scatter ? (int64_t)g.store_scatter[v] : v;
-    ((T *)g.dst)[db + dr * g.ds[1] + t * g.ds[3]] = (T)x;
-  }
-}
+int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, bool wide);
+int launch_ntt_pass_fwd64(const NttArgs &a, int64_t nblocks, bool wide);
+int launch_ntt_pass_inv32(const NttArgs &a, int64_t nblocks, bool wide);
+int launch_ntt_pass_inv64(const NttArgs &a, int64_t nblocks, bool wide);
 
 // out[i, u, j, t] = src[i, perm[u], j, t] (forward NTT with a non-bijective
 // permutation after the two-pass transform)
@@ -287,26 +63,9 @@ __global__ void __launch_bounds__(256) ntt_gather_kernel(const T *src, int64_t s
 }
 
 // ----------------------------------------------------------- host side
-template <typename T, bool WIDE, bool INV>
-static int launch_pass(const NttArgs &a, int64_t nblocks) {
-  const size_t smem = (size_t)(1 << a.p) * a.C * sizeof(int64_t);
-  static bool attr_set = false;
-  if (!attr_set) {
-    HEAL_TRY_CUDA(
-        cudaFuncSetAttribute(ntt_pass_kernel<T, WIDE, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    attr_set = true;
-  }
-  ntt_pass_kernel<T, WIDE, INV><<<(unsigned)nblocks, kNttThreads, smem, stream()>>>(a);
-  return check_launch("ntt_pass");
-}
-
 static int launch_any(const NttArgs &a, int64_t nblocks, bool is32, bool wide, bool inv) {
-  if (is32) {
-    if (wide) return inv ? launch_pass<int32_t, true, true>(a, nblocks) : launch_pass<int32_t, true, false>(a, nblocks);
-    return inv ? launch_pass<int32_t, false, true>(a, nblocks) : launch_pass<int32_t, false, false>(a, nblocks);
-  }
-  if (wide) return inv ? launch_pass<int64_t, true, true>(a, nblocks) : launch_pass<int64_t, true, false>(a, nblocks);
-  return inv ? launch_pass<int64_t, false, true>(a, nblocks) : launch_pass<int64_t, false, false>(a, nblocks);
+  if (inv) return is32 ? launch_ntt_pass_inv32(a, nblocks, wide) : launch_ntt_pass_inv64(a, nblocks, wide);
+  return is32 ? launch_ntt_pass_fwd32(a, nblocks, wide) : launch_ntt_pass_fwd64(a, nblocks, wide);
 }
 
 static void set_strides(int64_t *dst, const heal_tensor &t) {

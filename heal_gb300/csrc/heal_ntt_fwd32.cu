@@ -1,0 +1,10 @@
+// heal_ntt_fwd32.cu — forward (Cooley-Tukey) pass kernels for int32_t tensors
+// (one translation unit per direction and element type so they compile in
+// parallel); see heal_ntt_kernels.cuh.
+#include "heal_ntt_launch.cuh"
+
+namespace heal {
+int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, bool wide) {
+  return launch_direction_typed<int32_t, false>(a, nblocks, wide);
+}
+}  // namespace heal

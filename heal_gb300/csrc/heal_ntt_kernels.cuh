@@ -1,0 +1,444 @@
+// heal_ntt_kernels.cuh — NTT / INTT pass kernels (included by heal_ntt*.cu).
+//
+// A pass kernel owns a tile of P = 2^LOGP points x C adjacent limbs of one
+// (i, j) slice and runs LOGP stages of HEAL's butterfly network on it (see
+// heal_ntt.cu for how the stages split into passes and why the twiddle of
+// every butterfly equals the reference's).
+//
+// Register-blocked form (P >= 16): each thread keeps 16 points of one
+// column in registers and runs up to 4 stages per step on them (a radix-16
+// group: every twiddle is loaded once per group of butterflies that share
+// it); between steps the points are exchanged through a shared-memory tile.
+// The tile index of point s is XOR-swizzled, s ^ ((s >> 4) & 15), so that
+// both the strided (s = r + 16j) and the blocked (s = 16r + j) access
+// patterns of a step hit distinct banks.
+//
+// A tile holding a negative value (or a call with negative twiddles / m_inv)
+// takes the exact path instead: the reference's per-step truncated `%` in
+// __int128 on the shared tile, one stage per barrier.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "heal_internal.h"
+
+namespace heal {
+
+enum { KIND_STRIDED = 0, KIND_BLOCK = 1 };
+
+struct NttArgs {
+  const void *src;
+  int64_t ss[4];
+  const void *old;  // INTT: previous result contents for rows no index maps to
+  int64_t os[4];
+  void *dst;
+  int64_t ds[4];
+  int64_t l, m, r, k;
+  int p, logC, C;
+  int kind;
+  int64_t nsets;      // sets (strided) or blocks per column
+  int64_t ngroups_t;  // ceil(k / C)
+  const int32_t *load_map;
+  const int32_t *store_gather;
+  const int32_t *store_scatter;
+  const void *tw_pairs;
+  const int *tw_neg;
+  const void *tw_raw;
+  int64_t tw_s0, tw_s1;
+  const int64_t *q;
+  const void *minv_pairs;
+  const int *minv_neg;
+  const void *minv_raw;
+  int64_t minv_s0;
+  int scale;
+  int canon_load;
+  int force_exact;
+};
+
+template <bool WIDE>
+struct Word;
+template <>
+struct Word<true> {
+  typedef uint64_t W;
+  typedef ulonglong2 Pair;
+};
+template <>
+struct Word<false> {
+  typedef uint32_t W;
+  typedef uint2 Pair;
+};
+
+template <bool WIDE>
+__device__ __forceinline__ typename Word<WIDE>::W mulw(typename Word<WIDE>::W y, typename Word<WIDE>::Pair pr,
+                                                        typename Word<WIDE>::W q) {
+  if (WIDE) return (typename Word<WIDE>::W)shoup64((uint64_t)y, (uint64_t)pr.x, (uint64_t)pr.y, (uint64_t)q);
+  return (typename Word<WIDE>::W)shoup32((uint32_t)y, (uint32_t)pr.x, (uint32_t)pr.y, (uint32_t)q);
+}
+
+__device__ __forceinline__ int64_t raw_any(const void *base, int64_t off, bool is32) {
+  return is32 ? (int64_t)((const int32_t *)base)[off] : ((const int64_t *)base)[off];
+}
+
+// shared-tile word index of point s, column c
+__device__ __forceinline__ int tidx(int s, int c, int logC) { return ((s ^ ((s >> 4) & 15)) << logC) + c; }
+
+struct TileCtx {
+  int64_t rset, i, j, t0, G;
+  int P, C, logC;
+  __device__ __forceinline__ int64_t row_of(const NttArgs &g, int s) const {
+    return g.kind == KIND_BLOCK ? rset * P + s : rset + (int64_t)s * g.nsets;
+  }
+};
+
+__device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
+  TileCtx x;
+  x.P = 1 << g.p;
+  x.C = g.C;
+  x.logC = g.logC;
+  const int64_t bid = blockIdx.x;
+  x.rset = bid % g.nsets;
+  const int64_t cg = bid / g.nsets;
+  const int64_t tg = cg % g.ngroups_t;
+  const int64_t ij = cg / g.ngroups_t;
+  x.j = ij % g.r;
+  x.i = ij / g.r;
+  x.t0 = tg * g.C;
+  x.G = g.kind == KIND_BLOCK ? g.nsets + x.rset : 1;
+  return x;
+}
+
+template <typename T>
+__device__ __forceinline__ int64_t load_point(const NttArgs &g, const TileCtx &x, int s, int64_t t) {
+  const int64_t v = x.row_of(g, s);
+  if (g.load_map) {
+    const int32_t sr = g.load_map[v];
+    if (sr < 0) return (int64_t)((const T *)g.old)[x.i * g.os[0] + v * g.os[1] + x.j * g.os[2] + t * g.os[3]];
+    return (int64_t)((const T *)g.src)[x.i * g.ss[0] + (int64_t)sr * g.ss[1] + x.j * g.ss[2] + t * g.ss[3]];
+  }
+  return (int64_t)((const T *)g.src)[x.i * g.ss[0] + v * g.ss[1] + x.j * g.ss[2] + t * g.ss[3]];
+}
+
+template <typename T>
+__device__ __forceinline__ void store_point(const NttArgs &g, const TileCtx &x, int s, int64_t t, int64_t val) {
+  const int64_t v = x.row_of(g, s);
+  const int64_t dr = g.store_scatter ? (int64_t)g.store_scatter[v] : v;
+  ((T *)g.dst)[x.i * g.ds[0] + dr * g.ds[1] + x.j * g.ds[2] + t * g.ds[3]] = (T)val;
+}
+
+// Values that need the reference's own arithmetic: negative ones, and for the
+// inverse loaded from user data also values >= q (its first butterfly forms
+// u + q - v, negative when v > u + q).  The forward NTT reduces those instead.
+template <bool INV>
+__device__ __forceinline__ bool needs_exact(const NttArgs &g, int64_t x, int64_t q) {
+  return x < 0 || (INV && g.canon_load && x >= q);
+}
+
+// ---------------------------------------------------------- exact path
+// The tile (raw values, tidx layout) through the reference's arithmetic,
+// one stage per barrier; then stored (with m_inv scaling / gather).
+template <typename T, bool INV>
+__device__ __noinline__ void exact_tile(const NttArgs &g, const TileCtx &x, int64_t *tile) {
+  const int P = x.P, C = x.C, logC = x.logC, p = g.p;
+  const bool is32 = sizeof(T) == 4;
+  const int nbf = (P >> 1) * C;
+  for (int st = 0; st < p; ++st) {
+    for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
+      const int c = b & (C - 1);
+      const int64_t t = x.t0 + c;
+      if (t >= g.k) continue;
+      const int jb = b >> logC;
+      int su, sv;
+      int64_t twidx;
+      if (!INV) {
+        const int hl = p - 1 - st;
+        const int grp = jb >> hl;
+        su = (grp << (hl + 1)) + (jb & ((1 << hl) - 1));
+        sv = su + (1 << hl);
+        twidx = (x.G << st) + grp;
+      } else {
+        const int grp = jb >> st;
+        su = (grp << (st + 1)) + (jb & ((1 << st) - 1));
+        sv = su + (1 << st);
+        twidx = x.G * (int64_t)(P >> (st + 1)) + grp;
+      }
+      const int64_t q = g.q[t];
+      const int64_t s = raw_any(g.tw_raw, t * g.tw_s0 + twidx * g.tw_s1, is32);
+      const int64_t u = tile[tidx(su, c, logC)];
+      const int64_t v = tile[tidx(sv, c, logC)];
+      int64_t nu, nv;
+      if (!INV) {
+        const int64_t vm = crem128((i128)v * s, q);
+        nu = crem128((i128)u + vm, q);
+        nv = crem128((i128)u + q - vm, q);
+      } else {
+        nu = crem128((i128)u + v, q);
+        nv = crem128(((i128)u + q - v) * s, q);
+      }
+      tile[tidx(su, c, logC)] = nu;
+      tile[tidx(sv, c, logC)] = nv;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
+    const int s = e >> logC, c = e & (C - 1);
+    const int64_t t = x.t0 + c;
+    if (t >= g.k) continue;
+    int64_t val = g.store_gather ? tile[tidx(g.store_gather[s], c, logC)] : tile[tidx(s, c, logC)];
+    if (g.scale) val = crem128((i128)val * raw_any(g.minv_raw, t * g.minv_s0, is32), g.q[t]);
+    store_point<T>(g, x, s, t, val);
+  }
+}
+
+// ------------------------------------------------------ generic (P < 16)
+template <typename T, bool WIDE, bool INV>
+__global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ NttArgs g) {
+  typedef typename Word<WIDE>::W W;
+  typedef typename Word<WIDE>::Pair Pair;
+  extern __shared__ __align__(16) int64_t tile[];
+  const TileCtx x = tile_ctx(g);
+  const int P = x.P, C = x.C, logC = x.logC;
+  int neg = 0;
+  for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
+    const int s = e >> logC, c = e & (C - 1);
+    const int64_t t = x.t0 + c;
+    if (t >= g.k) continue;
+    const int64_t v = load_point<T>(g, x, s, t);
+    neg |= needs_exact<INV>(g, v, g.q[t]);
+    tile[tidx(s, c, logC)] = v;
+  }
+  const bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
+                     (g.scale && g.minv_neg && *g.minv_neg);
+  if (exact) {
+    exact_tile<T, INV>(g, x, tile);
+    return;
+  }
+  const int nbf = (P >> 1) * C;
+  if (g.canon_load) {
+    for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
+      const int s = e >> logC, c = e & (C - 1);
+      const int64_t t = x.t0 + c;
+      if (t >= g.k) continue;
+      const uint64_t q = (uint64_t)g.q[t];
+      const uint64_t v = (uint64_t)tile[tidx(s, c, logC)];
+      if (v >= q) tile[tidx(s, c, logC)] = (int64_t)(v % q);
+    }
+    __syncthreads();
+  }
+  for (int st = 0; st < g.p; ++st) {
+    for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
+      const int c = b & (C - 1);
+      const int64_t t = x.t0 + c;
+      if (t >= g.k) continue;
+      const int jb = b >> logC;
+      int su, sv;
+      int64_t twidx;
+      if (!INV) {
+        const int hl = g.p - 1 - st;
+        const int grp = jb >> hl;
+        su = (grp << (hl + 1)) + (jb & ((1 << hl) - 1));
+        sv = su + (1 << hl);
+        twidx = (x.G << st) + grp;
+      } else {
+        const int grp = jb >> st;
+        su = (grp << (st + 1)) + (jb & ((1 << st) - 1));
+        sv = su + (1 << st);
+        twidx = x.G * (int64_t)(P >> (st + 1)) + grp;
+      }
+      const W q = (W)g.q[t];
+      const Pair pr = __ldg((const Pair *)g.tw_pairs + t * g.m + twidx);
+      const W u = (W)tile[tidx(su, c, logC)];
+      const W v = (W)tile[tidx(sv, c, logC)];
+      W nu, nv;
+      if (!INV) {
+        const W tv = mulw<WIDE>(v, pr, q);
+        nu = u + tv;
+        nu = nu >= q ? nu - q : nu;
+        nv = u >= tv ? u - tv : u + (q - tv);
+      } else {
+        nu = u + v;
+        nu = nu >= q ? nu - q : nu;
+        const W d = u >= v ? u - v : u + (q - v);
+        nv = mulw<WIDE>(d, pr, q);
+      }
+      tile[tidx(su, c, logC)] = (int64_t)nu;
+      tile[tidx(sv, c, logC)] = (int64_t)nv;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
+    const int s = e >> logC, c = e & (C - 1);
+    const int64_t t = x.t0 + c;
+    if (t >= g.k) continue;
+    int64_t val = g.store_gather ? tile[tidx(g.store_gather[s], c, logC)] : tile[tidx(s, c, logC)];
+    if (g.scale) {
+      const Pair pr = __ldg((const Pair *)g.minv_pairs + t);
+      val = (int64_t)mulw<WIDE>((W)val, pr, (W)g.q[t]);
+    }
+    store_point<T>(g, x, s, t, val);
+  }
+}
+
+// --------------------------------------------------- register-blocked
+// Point held in register e (0..15) by thread r during step `step`.
+template <bool INV, int LOGP>
+__device__ __forceinline__ int point_of(int step, int r, int e) {
+  const int st0 = 4 * step;
+  const int q = (LOGP - st0) < 4 ? (LOGP - st0) : 4;
+  const int jj = e & ((1 << q) - 1);
+  const int id = (r << (4 - q)) + (e >> q);  // set index
+  if (!INV) {
+    const int lD = LOGP - st0 - q;  // log2 of the set spacing D
+    const int hi = id >> lD, lo = id & ((1 << lD) - 1);
+    return (hi << (lD + q)) + lo + (jj << lD);
+  }
+  const int hi = id >> st0, lo = id & ((1 << st0) - 1);
+  return (hi << (st0 + q)) + lo + (jj << st0);
+}
+
+// One register step: stages [4*STEP, 4*STEP + qn) on the 16 >> qn sets of
+// 2^qn points this thread holds.
+template <bool WIDE, bool INV, int LOGP, int STEP>
+__device__ __forceinline__ void reg_step(typename Word<WIDE>::W (&v)[16], int r, int64_t G,
+                                         const typename Word<WIDE>::Pair *twp, typename Word<WIDE>::W q) {
+  typedef typename Word<WIDE>::W W;
+  typedef typename Word<WIDE>::Pair Pair;
+  constexpr int P = 1 << LOGP;
+  constexpr int st0 = 4 * STEP;
+  constexpr int qn = (LOGP - st0) < 4 ? (LOGP - st0) : 4;
+#pragma unroll
+  for (int set = 0; set < (16 >> qn); ++set) {
+    const int id = (r << (4 - qn)) + set;
+    const int base = set << qn;
+#pragma unroll
+    for (int kk = 0; kk < qn; ++kk) {
+      const int st = st0 + kk;
+      if (!INV) {
+        constexpr int lD = LOGP - st0 - qn;
+        const int hi = id >> lD;
+        const int dist = 1 << (qn - 1 - kk);
+#pragma unroll
+        for (int gl = 0; gl < (1 << kk); ++gl) {
+          const Pair pr = __ldg(twp + (G << st) + ((int64_t)hi << kk) + gl);
+#pragma unroll
+          for (int off = 0; off < dist; ++off) {
+            const int a = base + gl * 2 * dist + off, b = a + dist;
+            const W tv = mulw<WIDE>(v[b], pr, q);
+            W nu = v[a] + tv;
+            nu = nu >= q ? nu - q : nu;
+            const W nv = v[a] >= tv ? v[a] - tv : v[a] + (q - tv);
+            v[a] = nu;
+            v[b] = nv;
+          }
+        }
+      } else {
+        const int hi = id >> st0;
+        const int dist = 1 << kk;
+#pragma unroll
+        for (int gl = 0; gl < (1 << (qn - 1 - kk)); ++gl) {
+          const Pair pr = __ldg(twp + G * (int64_t)(P >> (st + 1)) + ((int64_t)hi << (qn - 1 - kk)) + gl);
+#pragma unroll
+          for (int off = 0; off < dist; ++off) {
+            const int a = base + gl * 2 * dist + off, b = a + dist;
+            W nu = v[a] + v[b];
+            nu = nu >= q ? nu - q : nu;
+            const W d = v[a] >= v[b] ? v[a] - v[b] : v[a] + (q - v[b]);
+            v[a] = nu;
+            v[b] = mulw<WIDE>(d, pr, q);
+          }
+        }
+      }
+    }
+  }
+}
+
+// Steps STEP .. NSTEP-1, exchanging through the shared tile between steps.
+template <bool WIDE, bool INV, int LOGP, int STEP>
+__device__ __forceinline__ void reg_steps(typename Word<WIDE>::W (&v)[16], int r, int c, int logC, int64_t *tile,
+                                          int64_t G, const typename Word<WIDE>::Pair *twp,
+                                          typename Word<WIDE>::W q) {
+  typedef typename Word<WIDE>::W W;
+  constexpr int NSTEP = (LOGP + 3) / 4;
+  if constexpr (STEP < NSTEP) {
+    if constexpr (STEP > 0) {
+#pragma unroll
+      for (int e = 0; e < 16; ++e) tile[tidx(point_of<INV, LOGP>(STEP - 1, r, e), c, logC)] = (int64_t)v[e];
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < 16; ++e) v[e] = (W)tile[tidx(point_of<INV, LOGP>(STEP, r, e), c, logC)];
+      __syncthreads();
+    }
+    reg_step<WIDE, INV, LOGP, STEP>(v, r, G, twp, q);
+    reg_steps<WIDE, INV, LOGP, STEP + 1>(v, r, c, logC, tile, G, twp, q);
+  }
+}
+
+template <typename T, bool WIDE, bool INV, int LOGP>
+__global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
+  typedef typename Word<WIDE>::W W;
+  typedef typename Word<WIDE>::Pair Pair;
+  constexpr int NSTEP = (LOGP + 3) / 4;
+  extern __shared__ __align__(16) int64_t tile[];
+  const TileCtx x = tile_ctx(g);
+  const int logC = x.logC;
+  const int c = threadIdx.x & (x.C - 1);
+  const int r = threadIdx.x >> logC;
+  const int64_t t = x.t0 + c;
+  const bool act = t < g.k;
+  const int64_t tq = act ? t : g.k - 1;
+  const int64_t q64 = g.q[tq];
+
+  // ---- load (step-0 layout)
+  int64_t raw[16];
+  int neg = 0;
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    const int s = point_of<INV, LOGP>(0, r, e);
+    raw[e] = act ? load_point<T>(g, x, s, t) : 0;
+    neg |= needs_exact<INV>(g, raw[e], q64);
+  }
+  const bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
+                     (g.scale && g.minv_neg && *g.minv_neg);
+  if (exact) {
+#pragma unroll
+    for (int e = 0; e < 16; ++e) tile[tidx(point_of<INV, LOGP>(0, r, e), c, logC)] = raw[e];
+    __syncthreads();
+    exact_tile<T, INV>(g, x, tile);
+    return;
+  }
+
+  const W q = (W)q64;
+  const Pair *twp = (const Pair *)g.tw_pairs + tq * g.m;
+  W v[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    uint64_t u = (uint64_t)raw[e];
+    if (g.canon_load && u >= (uint64_t)q64) u %= (uint64_t)q64;
+    v[e] = (W)u;
+  }
+  reg_steps<WIDE, INV, LOGP, 0>(v, r, c, logC, tile, x.G, twp, q);
+
+  // ---- store
+  if (g.store_gather) {  // single-pass forward: out[u] = res[perm[u]]
+#pragma unroll
+    for (int e = 0; e < 16; ++e) tile[tidx(point_of<INV, LOGP>(NSTEP - 1, r, e), c, logC)] = (int64_t)v[e];
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int s = point_of<INV, LOGP>(0, r, e);
+        store_point<T>(g, x, s, t, tile[tidx(g.store_gather[s], c, logC)]);
+      }
+    }
+    return;
+  }
+  if (!act) return;
+  Pair mp;
+  if (g.scale) mp = __ldg((const Pair *)g.minv_pairs + t);
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    W val = v[e];
+    if (g.scale) val = mulw<WIDE>(val, mp, q);
+    store_point<T>(g, x, point_of<INV, LOGP>(NSTEP - 1, r, e), t, (int64_t)val);
+  }
+}
+
+}  // namespace heal

@@ -1,0 +1,55 @@
+// heal_ntt_launch.cuh — instantiates and launches the pass kernels of one
+// direction (included once by heal_ntt_fwd.cu and once by heal_ntt_inv.cu,
+// so the two directions compile in parallel).
+#pragma once
+#include "heal_ntt_kernels.cuh"
+
+namespace heal {
+
+template <typename Kern>
+static int launch_with_smem(Kern kern, const NttArgs &a, int64_t nblocks, int threads, size_t smem, bool &attr_set) {
+  if (!attr_set) {
+    HEAL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    attr_set = true;
+  }
+  kern<<<(unsigned)nblocks, threads, smem, stream()>>>(a);
+  return check_launch("ntt_pass");
+}
+
+template <typename T, bool WIDE, bool INV, int LOGP>
+static int launch_reg(const NttArgs &a, int64_t nblocks) {
+  static bool attr = false;
+  const int threads = ((1 << LOGP) / 16) * a.C;
+  const size_t smem = (size_t)(1 << LOGP) * a.C * sizeof(int64_t);
+  return launch_with_smem(ntt_reg_kernel<T, WIDE, INV, LOGP>, a, nblocks, threads, smem, attr);
+}
+
+template <typename T, bool WIDE, bool INV>
+static int launch_small(const NttArgs &a, int64_t nblocks) {
+  static bool attr = false;
+  const size_t smem = (size_t)(1 << a.p) * a.C * sizeof(int64_t);
+  return launch_with_smem(ntt_small_kernel<T, WIDE, INV>, a, nblocks, 256, smem, attr);
+}
+
+template <typename T, bool WIDE, bool INV>
+static int launch_typed(const NttArgs &a, int64_t nblocks) {
+  switch (a.p) {
+    case 4: return launch_reg<T, WIDE, INV, 4>(a, nblocks);
+    case 5: return launch_reg<T, WIDE, INV, 5>(a, nblocks);
+    case 6: return launch_reg<T, WIDE, INV, 6>(a, nblocks);
+    case 7: return launch_reg<T, WIDE, INV, 7>(a, nblocks);
+    case 8: return launch_reg<T, WIDE, INV, 8>(a, nblocks);
+    case 9: return launch_reg<T, WIDE, INV, 9>(a, nblocks);
+    case 10: return launch_reg<T, WIDE, INV, 10>(a, nblocks);
+    case 11: return launch_reg<T, WIDE, INV, 11>(a, nblocks);
+    case 12: return launch_reg<T, WIDE, INV, 12>(a, nblocks);
+    default: return launch_small<T, WIDE, INV>(a, nblocks);
+  }
+}
+
+template <typename T, bool INV>
+static int launch_direction_typed(const NttArgs &a, int64_t nblocks, bool wide) {
+  return wide ? launch_typed<T, true, INV>(a, nblocks) : launch_typed<T, false, INV>(a, nblocks);
+}
+
+}  // namespace heal
