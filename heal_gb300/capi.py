@@ -61,6 +61,7 @@ SIGNATURES = {
     "heal_modsum_ttc": ([_P, _P, _I64, _P], ctypes.c_int),
     "heal_modsum_tct": ([_P, _I64, _P, _P], ctypes.c_int),
     "heal_modsum_tcc": ([_P, _I64, _I64, _P], ctypes.c_int),
+    "heal_modmul_ttt_noalloc": ([_P, _P, _P, _P, _VP], ctypes.c_int),
     "heal_mod_tt": ([_P, _P, _P], ctypes.c_int),
     "heal_mod_tc": ([_P, _I64, _P], ctypes.c_int),
     "heal_mod_ct": ([_I64, _P, _P], ctypes.c_int),

@@ -19,6 +19,7 @@
 #include <string>
 #include <type_traits>
 #include <cstring>
+#include <mutex>
 
 #include "heal_internal.h"
 
@@ -176,6 +177,22 @@ __global__ void __launch_bounds__(256) modop_general_kernel(const __grid_constan
     int64_t p = P ? (int64_t)P[op] : g.ps;
     int64_t b = B ? (int64_t)B[ob] : g.bs;
     R[orr] = elem_op<T, OP>((int64_t)A[oa], b, p, c, g.diag);
+  }
+}
+
+// Reduction constants of every modulus element, written into a caller-given
+// array (the allocation-free modmul's fixed scratch).
+__global__ void mod_table_kernel_noalloc(const void *p, int dtype, View v, int64_t n, void *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t off = 0, idx = i;
+    for (int d = v.ndim - 1; d >= 0; --d) {
+      off += (idx % v.dims[d]) * v.strides[d];
+      idx /= v.dims[d];
+    }
+    if (dtype == HEAL_INT32)
+      ((MG32 *)out)[i] = mg32_make((int64_t)((const int32_t *)p)[off]);
+    else
+      ((MG64 *)out)[i] = mg64_make(((const int64_t *)p)[off]);
   }
 }
 
@@ -398,6 +415,131 @@ static int mod_ct(int64_t as, const heal_tensor *b, const heal_tensor *r) {
   return rc;
 }
 
+// ================================================ allocation-free modmul
+// Some callers cannot let a library allocate device memory: a serving
+// process that reserves HBM for its resident ciphertexts and keys up front
+// and fails any later cudaMalloc, a host runtime (Go, Java, ...) that owns
+// every device buffer through its own pool, or a latency-bound loop that
+// must not stall in the allocator.  heal_modmul_ttt_noalloc serves them:
+// the table it needs (the reduction constants of each modulus, which
+// heal_modmul_ttt caches in pool memory) lives in this fixed array instead.
+// Every GPU that loads the library keeps the array (128 KiB of constants and
+// one diagnostics record) until the process exits.
+constexpr int64_t kNoAllocMaxModuli = 4096;
+constexpr size_t kNoAllocTableBytes = (size_t)kNoAllocMaxModuli * sizeof(MG64);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocTableBytes + sizeof(Diag)];
+
+struct NoAllocDevice {
+  void *scratch = nullptr;  // device address of g_noalloc_scratch
+  int sms = 0;
+};
+static std::mutex g_noalloc_mu;
+static NoAllocDevice g_noalloc_dev[64];
+
+// First call on a device: resolve the array's device address (the host-side
+// symbol is not one) with that device current.  This happens on the first
+// call per device, which should come before any stream capture.
+static int noalloc_setup(NoAllocDevice **out) {
+  int dev = 0;
+  HEAL_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(HEAL_ERR_RUNTIME, "heal_modmul_ttt_noalloc: device ordinal above 63");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  NoAllocDevice &d = g_noalloc_dev[dev];
+  if (!d.scratch) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    HEAL_TRY_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
+    d.scratch = ptr;
+  }
+  *out = &d;
+  return HEAL_OK;
+}
+
+template <typename T>
+static int noalloc_launch(ModopArgs &g, bool dense, cudaStream_t s, int sms) {
+  auto grid = [&](int64_t work) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, (int64_t)std::max(sms, 1) * 8));
+  };
+  if (dense) {
+    const int vec = 16 / sizeof(T);
+    bool aligned = ((uintptr_t)g.ap % 16 == 0) && ((uintptr_t)g.rp % 16 == 0) && ((uintptr_t)g.bp % 16 == 0);
+    if (aligned)
+      modop_dense_kernel<T, OP_MUL, 16 / sizeof(T)><<<grid(g.n / vec + 1), 256, 0, s>>>(g);
+    else
+      modop_dense_kernel<T, OP_MUL, 1><<<grid(g.n), 256, 0, s>>>(g);
+  } else {
+    modop_general_kernel<T, OP_MUL><<<grid(g.n), 256, 0, s>>>(g);
+  }
+  return check_launch("modmul_ttt_noalloc");
+}
+
+static int modmul_noalloc(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *r,
+                          void *stream_ptr) {
+  clear_error();
+  HEAL_CHECK(check_desc(a, "a", true));
+  HEAL_CHECK(check_desc(b, "b", true));
+  HEAL_CHECK(check_desc(p, "p", true));
+  HEAL_CHECK(check_desc(r, "result", true));
+  const int dt = r->dtype;
+  if (a->dtype != dt || b->dtype != dt || p->dtype != dt)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "all tensors must have the element type of result");
+  HEAL_CHECK(check_bcast(*a, *r, "a"));
+  HEAL_CHECK(check_bcast(*b, *r, "b"));
+  HEAL_CHECK(check_p(*p, *r));
+  const int64_t np = numel(*p);
+  if (np > kNoAllocMaxModuli)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_modmul_ttt_noalloc: p has " + std::to_string(np) +
+                                                    " elements; at most 4096 are supported");
+  for (const heal_tensor *in : {a, b, p})
+    if (overlaps(*in, *r) && !identical_view(*in, *r))
+      return set_error(HEAL_ERR_INVALID_ARGUMENT,
+                       "heal_modmul_ttt_noalloc: result overlaps an input in another layout (that needs a copy)");
+  const int64_t n = numel(*r);
+  if (n == 0) return HEAL_OK;
+  NoAllocDevice *dev = nullptr;
+  HEAL_CHECK(noalloc_setup(&dev));
+  cudaStream_t s = (cudaStream_t)stream_ptr;
+  unsigned char *scratch = (unsigned char *)dev->scratch;
+
+  // the constants of this call's moduli, written over the previous call's
+  const int threads = 128;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((np + threads - 1) / threads, 1024));
+  mod_table_kernel_noalloc<<<blocks, threads, 0, s>>>(p->data, p->dtype, make_view(*p), np, scratch);
+  HEAL_CHECK(check_launch("modmul_ttt_noalloc constants"));
+
+  ModopArgs g;
+  memset(&g, 0, sizeof g);
+  g.r = make_view(*r);
+  g.a = bcast_view(*a, *r);
+  g.b = bcast_view(*b, *r);
+  g.p = bcast_view(*p, *r);
+  g.pd = bcast_dense_view(*p, *r);
+  g.ap = a->data;
+  g.bp = b->data;
+  g.pp = p->data;
+  g.rp = r->data;
+  g.ptab = scratch;
+  g.n = n;
+  g.diag = (Diag *)(scratch + kNoAllocTableBytes);  // written, never read back here
+  g.last = r->ndim ? r->dims[r->ndim - 1] : 1;
+  bool dense = dense_rowmajor(*r) && same_dims(*a, *r) && dense_rowmajor(*a) && same_dims(*b, *r) &&
+               dense_rowmajor(*b) && n < (int64_t)UINT32_MAX && r->ndim > 0;
+  if (dense) {
+    bool vec_last = p->ndim == 1 && (p->dims[0] == 1 || g.last <= p->dims[0]);
+    dense = vec_last && p->strides[0] == 1;
+    g.p_per_last = vec_last && p->dims[0] != 1;
+  }
+  if (dense && g.last > 0 && g.last < (int64_t)UINT32_MAX)
+    g.last_div = fastdiv_make((uint32_t)g.last);
+  else
+    dense = dense && !g.p_per_last;
+  int rc = dt == HEAL_INT32 ? noalloc_launch<int32_t>(g, dense, s, dev->sms)
+                            : noalloc_launch<int64_t>(g, dense, s, dev->sms);
+  if (!rc) mark_written(r->data);
+  return rc;
+}
+
 }  // namespace heal
 
 using namespace heal;
@@ -455,6 +597,10 @@ int heal_mod_tc(const heal_tensor *a, int64_t b, const heal_tensor *r) {
 int heal_mod_ct(int64_t a, const heal_tensor *b, const heal_tensor *r) {
   if (!b) return set_error(HEAL_ERR_INVALID_ARGUMENT, "b pointer must not be null.");
   return mod_ct(a, b, r);
+}
+int heal_modmul_ttt_noalloc(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p,
+                            const heal_tensor *result, void *stream) {
+  return modmul_noalloc(a, b, p, result, stream);
 }
 
 }  // extern "C"

@@ -159,6 +159,22 @@ int heal_mod_tt(const heal_tensor *a, const heal_tensor *b, const heal_tensor *r
 int heal_mod_tc(const heal_tensor *a, int64_t b, const heal_tensor *result);
 int heal_mod_ct(int64_t a, const heal_tensor *b, const heal_tensor *result);
 
+/* modmul_ttt without any device allocation, for callers that cannot let a
+ * library allocate: a serving process that reserves HBM up front and fails
+ * later allocations, a foreign host runtime that owns every device buffer,
+ * a loop that must not stall in an allocator.  No counterpart in HEAL.
+ * Same result as heal_modmul_ttt, on the caller's `stream` (a cudaStream_t;
+ * NULL is the default stream).  The moduli's reduction constants go to one
+ * fixed device array of this library (at most 4096 moduli: p with more
+ * elements is rejected with HEAL_ERR_INVALID_ARGUMENT), which every GPU that
+ * loads the library keeps until the process exits.  The first call on a
+ * device looks up that array's device address; make it before any stream
+ * capture.  All calls share the array and each overwrites it, so calls that
+ * overlap on the GPU (on different streams) race.  A result that overlaps
+ * an input in another layout is rejected (it would need a temporary copy). */
+int heal_modmul_ttt_noalloc(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p,
+                            const heal_tensor *result, void *stream);
+
 /* Extension (DeviceDispatcher._modneg_tt / _modneg_tc,
  * device_interface.py:51-54, which have no backend in HEAL):
  * result = (p - a % p) % p in the double-width type, broadcasting like
