@@ -246,6 +246,26 @@ def our_arm(args):
     traffic = profile_traffic()
     chain_bytes = ch.bytes_per_chain()
 
+    # ---- per-call split of one chain step (CUDA events around each HEAL call)
+    names = ["intt", "g_decomposition", "ntt", "modmul_ttt", "axis_modsum", "permute"]
+    d = ch.dev
+    calls = [lambda s: capi.call("heal_intt", cts[s % RING], d["p"], d["perm"], d["itw"], d["minv"], None, None, ch.x),
+             lambda s: capi.call("heal_g_decomposition", ch.x, ch.dig, D, BITS),
+             lambda s: capi.call("heal_ntt", ch.dig_flat, d["p_t"], d["perm"], d["tw_t"], None, None, ch.dn),
+             lambda s: capi.call("heal_modmul_ttt", ch.dn, d["key"], d["p_t"], ch.dn),
+             lambda s: capi.call("heal_axis_modsum", ch.prod_moved, d["p"], ch.acc, 3),
+             lambda s: capi.call("heal_permute", ch.acc, d["gal"], outs[s % RING], 2, 1)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(calls) + 1)] for _ in range(args.steps)]
+    barrier()
+    for s in range(args.steps):
+        evs[s][0].record(stream)
+        for ci, fn in enumerate(calls):
+            fn(s)
+            evs[s][ci + 1].record(stream)
+    torch.cuda.synchronize()
+    split_ms = {n: statistics.median(evs[s][ci].elapsed_time(evs[s][ci + 1]) for s in range(args.steps))
+                for ci, n in enumerate(names)}
+
     # ---- end to end through the C ABI from pinned host memory
     nbytes = 2 * N * L * 8
     import ctypes
@@ -292,6 +312,7 @@ def our_arm(args):
                              "traffic": traffic.get("bytes_per_call") if traffic else None},
                 "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
                 "gpu_launches": launches, "launches_per_step": launches / args.steps,
+                "split_ms": split_ms,
                 "clocks": clocks, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     if world > 1:

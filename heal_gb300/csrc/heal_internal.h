@@ -94,6 +94,7 @@ int mod_info(const heal_tensor &p, ModInfo *out);
 // when some twiddle is negative (the exact path is then taken).
 struct TwiddleTable {
   const void *pairs;
+  const int32_t *rowmap;  // limb -> row of `pairs`; rows of equal content are stored once (null: identity)
   const int *neg_flag;
   int wide;
 };

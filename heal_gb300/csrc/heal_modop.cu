@@ -110,44 +110,94 @@ struct VecOf {
 };
 
 // ------------------------------------------------------ dense kernel
-// result, a (and b) row-major with result's shape; VEC elements per step.
-template <typename T, int OP, int VEC>
+// result, a (and b) row-major with result's shape; VEC elements per vector,
+// two vectors per iteration.  With HOIST the grid stride is a multiple of
+// the modulus period (`last`), so every thread keeps the same moduli for its
+// whole run and loads their constants once.
+template <typename T, int OP, int VEC, bool HOIST>
 __global__ void __launch_bounds__(256) modop_dense_kernel(const __grid_constant__ ModopArgs g) {
   typedef typename VecOf<T>::type V;
+  typedef typename MGOf<T>::type M;
   const T *A = (const T *)g.ap;
   const T *B = (const T *)g.bp;
   T *R = (T *)g.rp;
   const int64_t nvec = g.n / VEC;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t base = v * VEC;
-    T av[VEC], bv[VEC], rv[VEC];
-    if (VEC == 1) {
-      av[0] = A[base];
-      if (B) bv[0] = B[base];
-    } else {
-      *(V *)av = __ldcs((const V *)(A + base));
-      if (B) *(V *)bv = __ldcs((const V *)(B + base));
-    }
-    uint32_t col = 0;
-    if (g.p_per_last) col = (uint32_t)base - fastdiv((uint32_t)base, g.last_div) * (uint32_t)g.last;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  auto col_of = [&](int64_t e) -> uint32_t {
+    return g.p_per_last ? (uint32_t)e - fastdiv((uint32_t)e, g.last_div) * (uint32_t)g.last : 0u;
+  };
+  M cst[VEC];
+  int64_t qv[VEC];
+  if (HOIST) {
+    uint32_t col = col_of(v * VEC);
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
-      typename MGOf<T>::type c = mg_of<T>(g, col);
-      int64_t b = B ? (int64_t)bv[j] : g.bs;
-      rv[j] = elem_op<T, OP>((int64_t)av[j], b, q_of<T>(g, c), c, g.diag);
+      cst[j] = mg_of<T>(g, col);
+      qv[j] = q_of<T>(g, cst[j]);
       if (g.p_per_last && ++col == (uint32_t)g.last) col = 0;
     }
-    if (VEC == 1) {
-      R[base] = rv[0];
-    } else {
-      __stcs((V *)(R + base), *(const V *)rv);
+  }
+  auto compute = [&](int64_t base, const T *av, const T *bv, T *rv) {
+    uint32_t col = HOIST ? 0u : col_of(base);
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+      const int64_t b = B ? (int64_t)bv[j] : g.bs;
+      if (HOIST) {
+        rv[j] = elem_op<T, OP>((int64_t)av[j], b, qv[j], cst[j], g.diag);
+      } else {
+        const M c = mg_of<T>(g, col);
+        rv[j] = elem_op<T, OP>((int64_t)av[j], b, q_of<T>(g, c), c, g.diag);
+        if (g.p_per_last && ++col == (uint32_t)g.last) col = 0;
+      }
     }
+  };
+  for (; v + stride < nvec; v += 2 * stride) {
+    T a0[VEC], a1[VEC], b0[VEC], b1[VEC], r0[VEC], r1[VEC];
+    if (VEC == 1) {
+      a0[0] = A[v];
+      a1[0] = A[v + stride];
+      if (B) {
+        b0[0] = B[v];
+        b1[0] = B[v + stride];
+      }
+    } else {
+      *(V *)a0 = *(const V *)(A + v * VEC);
+      *(V *)a1 = *(const V *)(A + (v + stride) * VEC);
+      if (B) {
+        *(V *)b0 = *(const V *)(B + v * VEC);
+        *(V *)b1 = *(const V *)(B + (v + stride) * VEC);
+      }
+    }
+    compute(v * VEC, a0, b0, r0);
+    compute((v + stride) * VEC, a1, b1, r1);
+    if (VEC == 1) {
+      R[v] = r0[0];
+      R[v + stride] = r1[0];
+    } else {
+      *(V *)(R + v * VEC) = *(const V *)r0;
+      *(V *)(R + (v + stride) * VEC) = *(const V *)r1;
+    }
+  }
+  if (v < nvec) {
+    T a0[VEC], b0[VEC], r0[VEC];
+    if (VEC == 1) {
+      a0[0] = A[v];
+      if (B) b0[0] = B[v];
+    } else {
+      *(V *)a0 = *(const V *)(A + v * VEC);
+      if (B) *(V *)b0 = *(const V *)(B + v * VEC);
+    }
+    compute(v * VEC, a0, b0, r0);
+    if (VEC == 1)
+      R[v] = r0[0];
+    else
+      *(V *)(R + v * VEC) = *(const V *)r0;
   }
   // tail (n not a multiple of VEC)
   if (VEC > 1 && blockIdx.x == 0 && (int64_t)threadIdx.x < g.n % VEC) {
     int64_t i = nvec * VEC + threadIdx.x;
-    int64_t col = g.p_per_last ? i % g.last : 0;
-    typename MGOf<T>::type c = mg_of<T>(g, col);
+    const M c = mg_of<T>(g, col_of(i));
     int64_t b = B ? (int64_t)B[i] : g.bs;
     R[i] = elem_op<T, OP>((int64_t)A[i], b, q_of<T>(g, c), c, g.diag);
   }
@@ -259,17 +309,42 @@ static int check_p(const heal_tensor &p, const heal_tensor &r) {
   return HEAL_OK;
 }
 
+// Blocks for the dense kernel: about `want`, rounded to a multiple of the
+// modulus period so that every thread keeps its moduli (0 when impossible).
+static int64_t hoist_blocks(int64_t last, int vec, int64_t want) {
+  if (last <= 0) return 0;
+  int64_t per = 256 * (int64_t)vec, a = last, b = per;
+  while (b) {
+    int64_t t = a % b;
+    a = b;
+    b = t;
+  }
+  const int64_t unit = last / a;  // blocks per period
+  if (unit > want) return 0;
+  return (want / unit) * unit;
+}
+
+template <typename T, int OP, int VEC>
+static void launch_dense(ModopArgs &g, cudaStream_t s, int64_t want_blocks) {
+  const int64_t vecs = (g.n / VEC + 1) / 2 + 1;  // two vectors per thread per iteration
+  const int64_t want = std::max<int64_t>(1, std::min<int64_t>(want_blocks, (vecs + 255) / 256));
+  const int64_t hb = g.p_per_last ? hoist_blocks(g.last, VEC, want_blocks) : want;
+  if (hb > 0)
+    modop_dense_kernel<T, OP, VEC, true><<<(unsigned)hb, 256, 0, s>>>(g);
+  else
+    modop_dense_kernel<T, OP, VEC, false><<<(unsigned)want, 256, 0, s>>>(g);
+}
+
 template <typename T, int OP>
 static int launch(ModopArgs &g, bool dense) {
   cudaStream_t s = stream();
   if (dense) {
-    const int vec = 16 / sizeof(T);
     bool aligned = ((uintptr_t)g.ap % 16 == 0) && ((uintptr_t)g.rp % 16 == 0) && (!g.bp || (uintptr_t)g.bp % 16 == 0);
-    if (aligned) {
-      modop_dense_kernel<T, OP, 16 / sizeof(T)><<<grid_for(g.n / vec + 1, 256, 8), 256, 0, s>>>(g);
-    } else {
-      modop_dense_kernel<T, OP, 1><<<grid_for(g.n, 256, 8), 256, 0, s>>>(g);
-    }
+    const int64_t want = (int64_t)std::max(device_sm_count(), 1) * 8;
+    if (aligned)
+      launch_dense<T, OP, 16 / sizeof(T)>(g, s, want);
+    else
+      launch_dense<T, OP, 1>(g, s, want);
   } else {
     modop_general_kernel<T, OP><<<grid_for(g.n, 256, 8), 256, 0, s>>>(g);
   }
@@ -464,10 +539,12 @@ static int noalloc_launch(ModopArgs &g, bool dense, cudaStream_t s, int sms) {
   if (dense) {
     const int vec = 16 / sizeof(T);
     bool aligned = ((uintptr_t)g.ap % 16 == 0) && ((uintptr_t)g.rp % 16 == 0) && ((uintptr_t)g.bp % 16 == 0);
+    const int64_t want = (int64_t)std::max(sms, 1) * 8;
+    (void)vec;
     if (aligned)
-      modop_dense_kernel<T, OP_MUL, 16 / sizeof(T)><<<grid(g.n / vec + 1), 256, 0, s>>>(g);
+      launch_dense<T, OP_MUL, 16 / sizeof(T)>(g, s, want);
     else
-      modop_dense_kernel<T, OP_MUL, 1><<<grid(g.n), 256, 0, s>>>(g);
+      launch_dense<T, OP_MUL, 1>(g, s, want);
   } else {
     modop_general_kernel<T, OP_MUL><<<grid(g.n), 256, 0, s>>>(g);
   }

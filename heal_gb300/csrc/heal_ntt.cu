@@ -40,10 +40,10 @@ namespace heal {
 
 constexpr int kSinglePassLogMax = 12;  // m <= 4096 in one pass
 
-int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, bool wide);
-int launch_ntt_pass_fwd64(const NttArgs &a, int64_t nblocks, bool wide);
-int launch_ntt_pass_inv32(const NttArgs &a, int64_t nblocks, bool wide);
-int launch_ntt_pass_inv64(const NttArgs &a, int64_t nblocks, bool wide);
+int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, int mode);
+int launch_ntt_pass_fwd64(const NttArgs &a, int64_t nblocks, int mode);
+int launch_ntt_pass_inv32(const NttArgs &a, int64_t nblocks, int mode);
+int launch_ntt_pass_inv64(const NttArgs &a, int64_t nblocks, int mode);
 
 // out[i, u, j, t] = src[i, perm[u], j, t] (forward NTT with a non-bijective
 // permutation after the two-pass transform)
@@ -63,9 +63,9 @@ __global__ void __launch_bounds__(256) ntt_gather_kernel(const T *src, int64_t s
 }
 
 // ----------------------------------------------------------- host side
-static int launch_any(const NttArgs &a, int64_t nblocks, bool is32, bool wide, bool inv) {
-  if (inv) return is32 ? launch_ntt_pass_inv32(a, nblocks, wide) : launch_ntt_pass_inv64(a, nblocks, wide);
-  return is32 ? launch_ntt_pass_fwd32(a, nblocks, wide) : launch_ntt_pass_fwd64(a, nblocks, wide);
+static int launch_any(const NttArgs &a, int64_t nblocks, bool is32, int mode, bool inv) {
+  if (inv) return is32 ? launch_ntt_pass_inv32(a, nblocks, mode) : launch_ntt_pass_inv64(a, nblocks, mode);
+  return is32 ? launch_ntt_pass_fwd32(a, nblocks, mode) : launch_ntt_pass_fwd64(a, nblocks, mode);
 }
 
 static void set_strides(int64_t *dst, const heal_tensor &t) {
@@ -119,7 +119,11 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   ModInfo mi;
   HEAL_CHECK(mod_info(*p, &mi));
   if (mi.min_q <= 0) return set_error(HEAL_ERR_RUNTIME, "moduli must be positive");
-  const bool wide = mi.max_q > 0x7FFFFFFF;
+  // arithmetic mode from the largest modulus (heal_ntt_kernels.cuh)
+  const int mode = mi.max_q < (int64_t(1) << 30)   ? MODE_N32_LAZY
+                   : mi.max_q < (int64_t(1) << 31) ? MODE_N32
+                                                   : MODE_W64_LAZY;
+  const bool wide = mode == MODE_W64_LAZY;
   PermInfo pi;
   HEAL_CHECK(perm_info(*perm, &pi));
   if (pi.bad) return set_error(HEAL_ERR_OUT_OF_RANGE, "Index out of bounds.");
@@ -138,6 +142,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   base.r = r;
   base.k = k;
   base.tw_pairs = tt.pairs;
+  base.tw_rowmap = tt.rowmap;
   base.tw_neg = tt.neg_flag;
   base.tw_raw = tw->data;
   base.tw_s0 = tw->strides[0];
@@ -149,7 +154,9 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
     base.minv_raw = minv->data;
     base.minv_s0 = minv->strides[0];
   }
-  base.force_exact = m == 1;
+  // m = 1 has no butterflies (the forward NTT is a plain copy, unreduced);
+  // moduli >= 2^62 do not fit the 64-bit lazy ranges
+  base.force_exact = m == 1 || mi.max_q >= (int64_t(1) << 62);
   const bool is32 = dt == HEAL_INT32;
   int C = 8;
   while (C > 1 && C / 2 >= k) C /= 2;
@@ -157,8 +164,9 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   void *tmp = nullptr, *tmp2 = nullptr;
 
   auto cfg = [&](NttArgs &x, int pbits, int kind) -> int64_t {
+    // at most 512 threads per CTA: P * C / kPT <= 512
     int c = C;
-    while (c > 1 && ((int64_t)1 << pbits) * c > 8192) c /= 2;
+    while (c > 1 && ((int64_t)1 << pbits) * c > 512 * kPT) c /= 2;
     x.p = pbits;
     x.C = c;
     x.logC = ilog2(c);
@@ -184,7 +192,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
     } else {
       x.store_gather = pi.perm32;
     }
-    rc = launch_any(x, nb, is32, wide, inv);
+    rc = launch_any(x, nb, is32, mode, inv);
   } else {
     // two passes through a dense [l, m, r, k] scratch tensor
     const int p1 = logm / 2, p2 = logm - p1;
@@ -204,7 +212,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
       x.dst = T1.data;
       set_strides(x.ds, T1);
       x.canon_load = 1;
-      rc = launch_any(x, nb, is32, wide, false);
+      rc = launch_any(x, nb, is32, mode, false);
       if (!rc) {
         NttArgs y = base;  // pass 2: remaining stages on contiguous blocks
         nb = cfg(y, p2, KIND_BLOCK);
@@ -214,14 +222,14 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
           y.dst = res->data;
           set_strides(y.ds, *res);
           y.store_scatter = pi.inv32;
-          rc = launch_any(y, nb, is32, wide, false);
+          rc = launch_any(y, nb, is32, mode, false);
         } else {
           heal_tensor T2 = T1;
           rc = scratch_alloc((size_t)s * elem_size(dt), &tmp2);
           T2.data = tmp2;
           y.dst = T2.data;
           set_strides(y.ds, T2);
-          if (!rc) rc = launch_any(y, nb, is32, wide, false);
+          if (!rc) rc = launch_any(y, nb, is32, mode, false);
           if (!rc) {
             int64_t n = l * m * r * k;
             int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 16);
@@ -250,7 +258,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
       x.dst = T1.data;
       set_strides(x.ds, T1);
       x.canon_load = 1;
-      rc = launch_any(x, nb, is32, wide, true);
+      rc = launch_any(x, nb, is32, mode, true);
       if (!rc) {
         NttArgs y = base;  // pass 2: remaining stages on strided sets, then m_inv
         nb = cfg(y, p2, KIND_STRIDED);
@@ -259,7 +267,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
         y.dst = res->data;
         set_strides(y.ds, *res);
         y.scale = 1;
-        rc = launch_any(y, nb, is32, wide, true);
+        rc = launch_any(y, nb, is32, mode, true);
       }
     }
   }

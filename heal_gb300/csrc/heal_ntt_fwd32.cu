@@ -4,7 +4,7 @@
 #include "heal_ntt_launch.cuh"
 
 namespace heal {
-int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, bool wide) {
-  return launch_direction_typed<int32_t, false>(a, nblocks, wide);
+int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, int mode) {
+  return launch_direction_typed<int32_t, false>(a, nblocks, mode);
 }
 }  // namespace heal

@@ -25,6 +25,14 @@ namespace heal {
 
 enum { KIND_STRIDED = 0, KIND_BLOCK = 1 };
 
+// log2 of the points one thread of the register kernel holds (a radix-2^kLPT
+// step per shared-memory exchange)
+#ifndef HEAL_NTT_LPT
+#define HEAL_NTT_LPT 3
+#endif
+constexpr int kLPT = HEAL_NTT_LPT;
+constexpr int kPT = 1 << kLPT;
+
 struct NttArgs {
   const void *src;
   int64_t ss[4];
@@ -41,6 +49,7 @@ struct NttArgs {
   const int32_t *store_gather;
   const int32_t *store_scatter;
   const void *tw_pairs;
+  const int32_t *tw_rowmap;  // limb -> row of tw_pairs (rows with equal content share one)
   const int *tw_neg;
   const void *tw_raw;
   int64_t tw_s0, tw_s1;
@@ -67,6 +76,23 @@ struct Word<false> {
   typedef uint2 Pair;
 };
 
+// Arithmetic modes of the register kernel:
+//   0  32-bit words, canonical values     (every q < 2^31)
+//   1  32-bit words, Harvey's lazy ranges (every q < 2^30: 4q < 2^32)
+//   2  64-bit words, Harvey's lazy ranges (every q < 2^62: 4q < 2^64)
+// Lazy butterflies keep forward values in [0, 4q) and inverse values in
+// [0, 2q) with one conditional subtraction per butterfly instead of three;
+// every pass still ends on canonical residues.
+enum { MODE_N32 = 0, MODE_N32_LAZY = 1, MODE_W64_LAZY = 2 };
+
+// y * w mod q up to one extra q: [0, 2q) for any y (Shoup, no final step)
+template <bool WIDE>
+__device__ __forceinline__ typename Word<WIDE>::W mulw_lazy(typename Word<WIDE>::W y, typename Word<WIDE>::Pair pr,
+                                                             typename Word<WIDE>::W q) {
+  if (WIDE) return (typename Word<WIDE>::W)((uint64_t)y * pr.x - mulhi64((uint64_t)y, pr.y) * (uint64_t)q);
+  return (typename Word<WIDE>::W)((uint32_t)y * pr.x - mulhi32((uint32_t)y, pr.y) * (uint32_t)q);
+}
+
 template <bool WIDE>
 __device__ __forceinline__ typename Word<WIDE>::W mulw(typename Word<WIDE>::W y, typename Word<WIDE>::Pair pr,
                                                         typename Word<WIDE>::W q) {
@@ -76,6 +102,12 @@ __device__ __forceinline__ typename Word<WIDE>::W mulw(typename Word<WIDE>::W y,
 
 __device__ __forceinline__ int64_t raw_any(const void *base, int64_t off, bool is32) {
   return is32 ? (int64_t)((const int32_t *)base)[off] : ((const int64_t *)base)[off];
+}
+
+template <typename Pair>
+__device__ __forceinline__ const Pair *tw_row(const NttArgs &g, int64_t t) {
+  const int64_t row = g.tw_rowmap ? (int64_t)g.tw_rowmap[t] : t;
+  return (const Pair *)g.tw_pairs + row * g.m;
 }
 
 // shared-tile word index of point s, column c
@@ -94,11 +126,14 @@ __device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
   x.P = 1 << g.p;
   x.C = g.C;
   x.logC = g.logC;
+  // (i, j) vary fastest: the CTAs that read the same twiddle rows (same
+  // limbs, same set) run back to back and share them through L2
   const int64_t bid = blockIdx.x;
-  x.rset = bid % g.nsets;
-  const int64_t cg = bid / g.nsets;
-  const int64_t tg = cg % g.ngroups_t;
-  const int64_t ij = cg / g.ngroups_t;
+  const int64_t nij = g.l * g.r;
+  const int64_t ij = bid % nij;
+  const int64_t rest = bid / nij;
+  x.rset = rest % g.nsets;
+  const int64_t tg = rest / g.nsets;
   x.j = ij % g.r;
   x.i = ij / g.r;
   x.t0 = tg * g.C;
@@ -244,7 +279,7 @@ __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ 
         twidx = x.G * (int64_t)(P >> (st + 1)) + grp;
       }
       const W q = (W)g.q[t];
-      const Pair pr = __ldg((const Pair *)g.tw_pairs + t * g.m + twidx);
+      const Pair pr = __ldg(tw_row<Pair>(g, t) + twidx);
       const W u = (W)tile[tidx(su, c, logC)];
       const W v = (W)tile[tidx(sv, c, logC)];
       W nu, nv;
@@ -278,13 +313,14 @@ __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ 
 }
 
 // --------------------------------------------------- register-blocked
-// Point held in register e (0..15) by thread r during step `step`.
+// Point held in register e (0 .. kPT-1) by thread r during step `step`
+// (steps of kLPT stages; the last one may be shorter).
 template <bool INV, int LOGP>
 __device__ __forceinline__ int point_of(int step, int r, int e) {
-  const int st0 = 4 * step;
-  const int q = (LOGP - st0) < 4 ? (LOGP - st0) : 4;
+  const int st0 = kLPT * step;
+  const int q = (LOGP - st0) < kLPT ? (LOGP - st0) : kLPT;
   const int jj = e & ((1 << q) - 1);
-  const int id = (r << (4 - q)) + (e >> q);  // set index
+  const int id = (r << (kLPT - q)) + (e >> q);  // set index
   if (!INV) {
     const int lD = LOGP - st0 - q;  // log2 of the set spacing D
     const int hi = id >> lD, lo = id & ((1 << lD) - 1);
@@ -294,19 +330,23 @@ __device__ __forceinline__ int point_of(int step, int r, int e) {
   return (hi << (st0 + q)) + lo + (jj << st0);
 }
 
-// One register step: stages [4*STEP, 4*STEP + qn) on the 16 >> qn sets of
-// 2^qn points this thread holds.
-template <bool WIDE, bool INV, int LOGP, int STEP>
-__device__ __forceinline__ void reg_step(typename Word<WIDE>::W (&v)[16], int r, int64_t G,
-                                         const typename Word<WIDE>::Pair *twp, typename Word<WIDE>::W q) {
+// One register step: stages [kLPT*STEP, kLPT*STEP + qn) on the kPT >> qn
+// sets of 2^qn points this thread holds.
+template <int MODE, bool INV, int LOGP, int STEP>
+__device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W (&v)[kPT], int r, int64_t G,
+                                         const typename Word<MODE == MODE_W64_LAZY>::Pair *twp,
+                                         typename Word<MODE == MODE_W64_LAZY>::W q) {
+  constexpr bool WIDE = MODE == MODE_W64_LAZY;
+  constexpr bool LAZY = MODE != MODE_N32;
   typedef typename Word<WIDE>::W W;
   typedef typename Word<WIDE>::Pair Pair;
   constexpr int P = 1 << LOGP;
-  constexpr int st0 = 4 * STEP;
-  constexpr int qn = (LOGP - st0) < 4 ? (LOGP - st0) : 4;
+  constexpr int st0 = kLPT * STEP;
+  constexpr int qn = (LOGP - st0) < kLPT ? (LOGP - st0) : kLPT;
+  const W q2 = q + q;
 #pragma unroll
-  for (int set = 0; set < (16 >> qn); ++set) {
-    const int id = (r << (4 - qn)) + set;
+  for (int set = 0; set < (kPT >> qn); ++set) {
+    const int id = (r << (kLPT - qn)) + set;
     const int base = set << qn;
 #pragma unroll
     for (int kk = 0; kk < qn; ++kk) {
@@ -321,12 +361,20 @@ __device__ __forceinline__ void reg_step(typename Word<WIDE>::W (&v)[16], int r,
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
             const int a = base + gl * 2 * dist + off, b = a + dist;
-            const W tv = mulw<WIDE>(v[b], pr, q);
-            W nu = v[a] + tv;
-            nu = nu >= q ? nu - q : nu;
-            const W nv = v[a] >= tv ? v[a] - tv : v[a] + (q - tv);
-            v[a] = nu;
-            v[b] = nv;
+            if (LAZY) {
+              W u = v[a];
+              u = u >= q2 ? u - q2 : u;
+              const W tv = mulw_lazy<WIDE>(v[b], pr, q);
+              v[a] = u + tv;
+              v[b] = u - tv + q2;
+            } else {
+              const W tv = mulw<WIDE>(v[b], pr, q);
+              W nu = v[a] + tv;
+              nu = nu >= q ? nu - q : nu;
+              const W nv = v[a] >= tv ? v[a] - tv : v[a] + (q - tv);
+              v[a] = nu;
+              v[b] = nv;
+            }
           }
         }
       } else {
@@ -338,11 +386,19 @@ __device__ __forceinline__ void reg_step(typename Word<WIDE>::W (&v)[16], int r,
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
             const int a = base + gl * 2 * dist + off, b = a + dist;
-            W nu = v[a] + v[b];
-            nu = nu >= q ? nu - q : nu;
-            const W d = v[a] >= v[b] ? v[a] - v[b] : v[a] + (q - v[b]);
-            v[a] = nu;
-            v[b] = mulw<WIDE>(d, pr, q);
+            if (LAZY) {
+              W s = v[a] + v[b];
+              s = s >= q2 ? s - q2 : s;
+              const W d = v[a] - v[b] + q2;
+              v[a] = s;
+              v[b] = mulw_lazy<WIDE>(d, pr, q);
+            } else {
+              W nu = v[a] + v[b];
+              nu = nu >= q ? nu - q : nu;
+              const W d = v[a] >= v[b] ? v[a] - v[b] : v[a] + (q - v[b]);
+              v[a] = nu;
+              v[b] = mulw<WIDE>(d, pr, q);
+            }
           }
         }
       }
@@ -351,31 +407,34 @@ __device__ __forceinline__ void reg_step(typename Word<WIDE>::W (&v)[16], int r,
 }
 
 // Steps STEP .. NSTEP-1, exchanging through the shared tile between steps.
-template <bool WIDE, bool INV, int LOGP, int STEP>
-__device__ __forceinline__ void reg_steps(typename Word<WIDE>::W (&v)[16], int r, int c, int logC, int64_t *tile,
-                                          int64_t G, const typename Word<WIDE>::Pair *twp,
-                                          typename Word<WIDE>::W q) {
-  typedef typename Word<WIDE>::W W;
-  constexpr int NSTEP = (LOGP + 3) / 4;
+template <int MODE, bool INV, int LOGP, int STEP>
+__device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::W (&v)[kPT], int r, int c, int logC,
+                                          int64_t *tile, int64_t G,
+                                          const typename Word<MODE == MODE_W64_LAZY>::Pair *twp,
+                                          typename Word<MODE == MODE_W64_LAZY>::W q) {
+  typedef typename Word<MODE == MODE_W64_LAZY>::W W;
+  constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
   if constexpr (STEP < NSTEP) {
     if constexpr (STEP > 0) {
 #pragma unroll
-      for (int e = 0; e < 16; ++e) tile[tidx(point_of<INV, LOGP>(STEP - 1, r, e), c, logC)] = (int64_t)v[e];
+      for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP>(STEP - 1, r, e), c, logC)] = (int64_t)v[e];
       __syncthreads();
 #pragma unroll
-      for (int e = 0; e < 16; ++e) v[e] = (W)tile[tidx(point_of<INV, LOGP>(STEP, r, e), c, logC)];
+      for (int e = 0; e < kPT; ++e) v[e] = (W)tile[tidx(point_of<INV, LOGP>(STEP, r, e), c, logC)];
       __syncthreads();
     }
-    reg_step<WIDE, INV, LOGP, STEP>(v, r, G, twp, q);
-    reg_steps<WIDE, INV, LOGP, STEP + 1>(v, r, c, logC, tile, G, twp, q);
+    reg_step<MODE, INV, LOGP, STEP>(v, r, G, twp, q);
+    reg_steps<MODE, INV, LOGP, STEP + 1>(v, r, c, logC, tile, G, twp, q);
   }
 }
 
-template <typename T, bool WIDE, bool INV, int LOGP>
+template <typename T, int MODE, bool INV, int LOGP>
 __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
+  constexpr bool WIDE = MODE == MODE_W64_LAZY;
+  constexpr bool LAZY = MODE != MODE_N32;
   typedef typename Word<WIDE>::W W;
   typedef typename Word<WIDE>::Pair Pair;
-  constexpr int NSTEP = (LOGP + 3) / 4;
+  constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
   extern __shared__ __align__(16) int64_t tile[];
   const TileCtx x = tile_ctx(g);
   const int logC = x.logC;
@@ -387,10 +446,10 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
   const int64_t q64 = g.q[tq];
 
   // ---- load (step-0 layout)
-  int64_t raw[16];
+  int64_t raw[kPT];
   int neg = 0;
 #pragma unroll
-  for (int e = 0; e < 16; ++e) {
+  for (int e = 0; e < kPT; ++e) {
     const int s = point_of<INV, LOGP>(0, r, e);
     raw[e] = act ? load_point<T>(g, x, s, t) : 0;
     neg |= needs_exact<INV>(g, raw[e], q64);
@@ -399,31 +458,41 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
                      (g.scale && g.minv_neg && *g.minv_neg);
   if (exact) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) tile[tidx(point_of<INV, LOGP>(0, r, e), c, logC)] = raw[e];
+    for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP>(0, r, e), c, logC)] = raw[e];
     __syncthreads();
     exact_tile<T, INV>(g, x, tile);
     return;
   }
 
   const W q = (W)q64;
-  const Pair *twp = (const Pair *)g.tw_pairs + tq * g.m;
-  W v[16];
+  const Pair *twp = tw_row<Pair>(g, tq);
+  W v[kPT];
 #pragma unroll
-  for (int e = 0; e < 16; ++e) {
+  for (int e = 0; e < kPT; ++e) {
     uint64_t u = (uint64_t)raw[e];
     if (g.canon_load && u >= (uint64_t)q64) u %= (uint64_t)q64;
     v[e] = (W)u;
   }
-  reg_steps<WIDE, INV, LOGP, 0>(v, r, c, logC, tile, x.G, twp, q);
+  reg_steps<MODE, INV, LOGP, 0>(v, r, c, logC, tile, x.G, twp, q);
+
+  // ---- back to canonical residues (forward values < 4q, inverse < 2q)
+  if (LAZY) {
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      W u = v[e];
+      if (!INV) u = u >= q + q ? u - (q + q) : u;
+      v[e] = u >= q ? u - q : u;
+    }
+  }
 
   // ---- store
   if (g.store_gather) {  // single-pass forward: out[u] = res[perm[u]]
 #pragma unroll
-    for (int e = 0; e < 16; ++e) tile[tidx(point_of<INV, LOGP>(NSTEP - 1, r, e), c, logC)] = (int64_t)v[e];
+    for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP>(NSTEP - 1, r, e), c, logC)] = (int64_t)v[e];
     __syncthreads();
     if (act) {
 #pragma unroll
-      for (int e = 0; e < 16; ++e) {
+      for (int e = 0; e < kPT; ++e) {
         const int s = point_of<INV, LOGP>(0, r, e);
         store_point<T>(g, x, s, t, tile[tidx(g.store_gather[s], c, logC)]);
       }
@@ -434,7 +503,7 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
   Pair mp;
   if (g.scale) mp = __ldg((const Pair *)g.minv_pairs + t);
 #pragma unroll
-  for (int e = 0; e < 16; ++e) {
+  for (int e = 0; e < kPT; ++e) {
     W val = v[e];
     if (g.scale) val = mulw<WIDE>(val, mp, q);
     store_point<T>(g, x, point_of<INV, LOGP>(NSTEP - 1, r, e), t, (int64_t)val);

@@ -5,17 +5,21 @@
 //                reference's order, sum = (sum + a_r) % q, so negative
 //                operands give the same truncated residues.
 //  g_decomposition (include/g_decomposition.h:24-30; g_decomposition_impl.cpp)
-//                one thread per input element writes its `power` digits;
-//                `value % base` and `value /= base` act on the value converted
-//                to uint64 (base is a size_t), the quotient stored back in T.
+//                on dense tensors one thread per 16-byte vector of inputs, its
+//                digits written as 16-byte stores; one thread per input element
+//                otherwise; `value % base` and
+//                `value /= base` act on the value converted to uint64 (base is
+//                a size_t), the quotient stored back in T.
 //  permute       (include/permute.h:33-40; permute_impl.cpp) a gather of
 //                whole rows along perm_axis.
-// All three are HBM-bound streams.
+// All three are HBM-bound streams; index arithmetic uses 32-bit invariant
+// division whenever the index space fits 32 bits.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "heal_internal.h"
 
@@ -47,6 +51,8 @@ struct AxisArgs {
   void *out;
   int64_t n;
   Diag *diag;
+  int fast;                       // n and every dim below 2^32: 32-bit index math
+  FastDiv fd[HEAL_MAX_DIMS];      // division by each result dim
 };
 
 template <typename T>
@@ -56,14 +62,27 @@ __global__ void __launch_bounds__(256) axis_modsum_kernel(const __grid_constant_
   T *R = (T *)g.out;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t rem = idx, oa = 0, orr = 0, last = 0;
-    for (int i = g.r.ndim - 1; i >= 0; --i) {
-      int64_t d = g.r.dims[i];
-      int64_t c = rem % d;
-      rem /= d;
-      if (i == g.r.ndim - 1) last = c;
-      oa += c * g.ai.strides[i];
-      orr += c * g.r.strides[i];
+    int64_t oa = 0, orr = 0, last = 0;
+    if (g.fast) {
+      uint32_t rem = (uint32_t)idx;
+      for (int i = g.r.ndim - 1; i >= 0; --i) {
+        const uint32_t qd = fastdiv(rem, g.fd[i]);
+        const int64_t c = rem - qd * (uint32_t)g.r.dims[i];
+        rem = qd;
+        if (i == g.r.ndim - 1) last = c;
+        oa += c * g.ai.strides[i];
+        orr += c * g.r.strides[i];
+      }
+    } else {
+      int64_t rem = idx;
+      for (int i = g.r.ndim - 1; i >= 0; --i) {
+        int64_t d = g.r.dims[i];
+        int64_t c = rem % d;
+        rem /= d;
+        if (i == g.r.ndim - 1) last = c;
+        oa += c * g.ai.strides[i];
+        orr += c * g.r.strides[i];
+      }
     }
     const int64_t q = (int64_t)P[last * g.p_stride];
     if (q == 0) {
@@ -131,6 +150,11 @@ static int axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_te
     g.out = r->data;
     g.n = n;
     g.diag = diag_device();
+    g.fast = n < (int64_t)UINT32_MAX;
+    for (int i = 0; i < r->ndim; ++i) {
+      if (r->dims[i] >= (int64_t)UINT32_MAX) g.fast = 0;
+      else g.fd[i] = fastdiv_make((uint32_t)std::max<int64_t>(r->dims[i], 1));
+    }
     if (r->dtype == HEAL_INT32)
       axis_modsum_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
     else
@@ -154,6 +178,63 @@ struct GdecArgs {
   int dense;       // a and result row-major
   Diag *diag;
 };
+
+// Digit d of `value` after d of the reference's steps (remainder and
+// quotient of the value as uint64, quotient stored back in T), in closed
+// form.  int64: the first quotient is already non-negative, so the steps are
+// logical shifts of the uint64 image.  int32: storing uv >> bits back into
+// an int32 is an arithmetic shift of the int32 value (saturating at 31).
+template <typename T>
+__device__ __forceinline__ uint64_t gdec_digit(int64_t value, uint64_t d, uint64_t bits, uint64_t mask) {
+  const uint64_t sh = d * bits;
+  if (sizeof(T) == 4) {
+    const int32_t v = (int32_t)value >> (sh > 31 ? 31 : sh);
+    return (uint64_t)(int64_t)v & mask;
+  }
+  const uint64_t uv = (uint64_t)value;
+  return (sh >= 64 ? 0 : (uv >> sh)) & mask;
+}
+
+// Dense layout, power PW <= 8: each thread decomposes the VEC elements of one
+// 16-byte vector and writes their VEC * PW digits as PW 16-byte stores.
+template <typename T, int PW>
+__global__ void __launch_bounds__(256) gdec_vec_kernel(const __grid_constant__ GdecArgs g) {
+  typedef typename std::conditional<sizeof(T) == 8, longlong2, int4>::type V;
+  constexpr int VEC = 16 / sizeof(T);
+  const T *A = (const T *)g.in;
+  T *R = (T *)g.out;
+  const uint64_t mask = g.bits >= 64 ? ~0ull : ((1ull << g.bits) - 1);
+  const int64_t nvec = g.n / VEC;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += (int64_t)gridDim.x * blockDim.x) {
+    T x[VEC], out[VEC * PW];
+    *(V *)x = *(const V *)(A + v * VEC);
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+#pragma unroll
+      for (int d = 0; d < PW; ++d) out[e * PW + d] = (T)(int64_t)gdec_digit<T>((int64_t)x[e], d, g.bits, mask);
+      const int64_t rest = (int64_t)gdec_digit<T>((int64_t)x[e], PW, g.bits, ~0ull);
+      // the residual after PW steps, as the reference's `value > 0` sees it
+      const int64_t resid = sizeof(T) == 4 ? (int64_t)(int32_t)(uint32_t)rest : rest;
+      if (resid > 0) {
+        unsigned long long slot = atomicAdd(&g.diag->count, 1ull);
+        if (slot < (unsigned long long)kDiagRecords) {
+          DiagRecord &rec = g.diag->rec[slot];
+          int64_t rem = v * VEC + e;
+          for (int i = g.a.ndim - 1; i >= 0; --i) {
+            rec.coord[i] = rem % g.a.dims[i];
+            rem /= g.a.dims[i];
+          }
+          rec.ndim = g.a.ndim;
+          rec.kind = 1;
+          rec.base_bits = g.bits;
+          rec.power = g.power;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < PW; ++k) *(V *)(R + v * VEC * PW + k * VEC) = *(const V *)(out + k * VEC);
+  }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) gdec_kernel(const __grid_constant__ GdecArgs g) {
@@ -233,10 +314,35 @@ static int g_decomposition(const heal_tensor *a, const heal_tensor *r, uint64_t 
     g.bits = bits;
     g.dense = dense_rowmajor(A) && dense_rowmajor(*r);
     g.diag = diag_device();
-    if (r->dtype == HEAL_INT32)
+    const int vec = 16 / elem_size(r->dtype);
+    const bool vec_ok = g.dense && power >= 1 && power <= 8 && bits < 64 && n % vec == 0 &&
+                        (r->dtype == HEAL_INT64 || bits <= 32) &&
+                        (uintptr_t)A.data % 16 == 0 && (uintptr_t)r->data % 16 == 0;
+    if (vec_ok) {
+      const int grid = grid_for(n / vec, 256, 8);
+#define HEAL_GDEC_CASE(PW)                                                                 \
+  case PW:                                                                                 \
+    if (r->dtype == HEAL_INT32)                                                            \
+      gdec_vec_kernel<int32_t, PW><<<grid, 256, 0, stream()>>>(g);                         \
+    else                                                                                   \
+      gdec_vec_kernel<int64_t, PW><<<grid, 256, 0, stream()>>>(g);                         \
+    break;
+      switch ((int)power) {
+        HEAL_GDEC_CASE(1)
+        HEAL_GDEC_CASE(2)
+        HEAL_GDEC_CASE(3)
+        HEAL_GDEC_CASE(4)
+        HEAL_GDEC_CASE(5)
+        HEAL_GDEC_CASE(6)
+        HEAL_GDEC_CASE(7)
+        HEAL_GDEC_CASE(8)
+      }
+#undef HEAL_GDEC_CASE
+    } else if (r->dtype == HEAL_INT32) {
       gdec_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
-    else
+    } else {
       gdec_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    }
     rc = check_launch("g_decomposition");
   }
   scratch_free(oa);
@@ -259,6 +365,8 @@ struct PermuteArgs {
   int64_t post;
   int64_t ew_div, ew_mod;  // ew coordinate = (x / ew_div) % l with x = pre or inner
   int ew_in_post;
+  int fast;                 // n below 2^32: 32-bit divisions below
+  FastDiv f_post, f_m, f_ewdiv, f_ewmod;
 };
 
 template <typename T>
@@ -269,11 +377,23 @@ __global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ Pe
        idx += (int64_t)gridDim.x * blockDim.x) {
     int64_t src, dst;
     if (g.dense) {
-      int64_t inner = idx % g.post;
-      int64_t rest = idx / g.post;
-      int64_t pm = rest % g.m;
-      int64_t pre = rest / g.m;
-      int64_t e = ((g.ew_in_post ? inner : pre) / g.ew_div) % g.ew_mod;
+      int64_t inner, pm, pre, e;
+      if (g.fast) {
+        const uint32_t x = (uint32_t)idx;
+        const uint32_t rest = fastdiv(x, g.f_post);
+        inner = x - rest * (uint32_t)g.post;
+        const uint32_t pr = fastdiv(rest, g.f_m);
+        pm = rest - pr * (uint32_t)g.m;
+        pre = pr;
+        const uint32_t y = fastdiv((uint32_t)(g.ew_in_post ? inner : pre), g.f_ewdiv);
+        e = y - fastdiv(y, g.f_ewmod) * (uint32_t)g.ew_mod;
+      } else {
+        inner = idx % g.post;
+        const int64_t rest = idx / g.post;
+        pm = rest % g.m;
+        pre = rest / g.m;
+        e = ((g.ew_in_post ? inner : pre) / g.ew_div) % g.ew_mod;
+      }
       int64_t pidx = g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[e * g.ps0 + pm * g.ps1]
                                                  : ((const int64_t *)g.perms)[e * g.ps0 + pm * g.ps1];
       src = (pre * g.m + pidx) * g.post + inner;
@@ -355,6 +475,14 @@ static int permute(const heal_tensor *a, const heal_tensor *perms, const heal_te
       }
       g.ew_div = div;
       g.ew_mod = l;
+      g.fast = n < (int64_t)UINT32_MAX && post < (int64_t)UINT32_MAX && m < (int64_t)UINT32_MAX &&
+               div < (int64_t)UINT32_MAX && l < (int64_t)UINT32_MAX && post > 0 && m > 0 && l > 0;
+      if (g.fast) {
+        g.f_post = fastdiv_make((uint32_t)post);
+        g.f_m = fastdiv_make((uint32_t)m);
+        g.f_ewdiv = fastdiv_make((uint32_t)div);
+        g.f_ewmod = fastdiv_make((uint32_t)l);
+      }
     }
     if (r->dtype == HEAL_INT32)
       permute_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);

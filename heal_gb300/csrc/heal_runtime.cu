@@ -467,7 +467,8 @@ struct TwArgs {
   int tw_dtype;
   int64_t tw_s0, tw_s1;
   const int64_t *q;
-  int64_t k, m;
+  const int32_t *rows;  // compact row -> source row (null: identity)
+  int64_t k, m;         // k = rows in the output table
   void *pairs;
   int *neg;
 };
@@ -476,7 +477,8 @@ template <bool WIDE>
 __global__ void twiddle_kernel(TwArgs a) {
   int64_t n = a.k * a.m;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t t = i / a.m, j = i - t * a.m;
+    int64_t u = i / a.m, j = i - u * a.m;
+    int64_t t = a.rows ? (int64_t)a.rows[u] : u;
     int64_t s = load_any(a.tw, a.tw_dtype, t * a.tw_s0 + j * a.tw_s1);
     int64_t q = a.q[t];
     if (s < 0) atomicOr(a.neg, 1);
@@ -496,8 +498,8 @@ __global__ void twiddle_kernel(TwArgs a) {
   }
 }
 
-static int build_pairs(const void *tw, int tw_dtype, int64_t s0, int64_t s1, const int64_t *q, int64_t k, int64_t m,
-                       int wide, CacheEntry &n) {
+static int build_pairs(const void *tw, int tw_dtype, int64_t s0, int64_t s1, const int64_t *q, const int32_t *rows,
+                       int64_t k, int64_t m, int wide, CacheEntry &n) {
   void *pairs, *flag;
   size_t es = wide ? sizeof(ulonglong2) : sizeof(uint2);
   HEAL_CHECK(scratch_alloc(std::max<int64_t>(k * m, 1) * es, &pairs));
@@ -506,7 +508,7 @@ static int build_pairs(const void *tw, int tw_dtype, int64_t s0, int64_t s1, con
   n.bufs.push_back(flag);
   HEAL_TRY_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), stream()));
   if (k * m) {
-    TwArgs a{tw, tw_dtype, s0, s1, q, k, m, pairs, (int *)flag};
+    TwArgs a{tw, tw_dtype, s0, s1, q, rows, k, m, pairs, (int *)flag};
     if (wide)
       twiddle_kernel<true><<<grid_for(k * m, 256), 256, 0, stream()>>>(a);
     else
@@ -514,6 +516,39 @@ static int build_pairs(const void *tw, int tw_dtype, int64_t s0, int64_t s1, con
     HEAL_CHECK(check_launch("twiddle_table"));
   }
   return HEAL_OK;
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x ^= x >> 30;
+  x *= 0xBF58476D1CE4E5B9ull;
+  x ^= x >> 27;
+  x *= 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// one block per twiddle row: an order-aware hash of the row and its modulus
+__global__ void row_hash_kernel(const void *tw, int dtype, int64_t s0, int64_t s1, const int64_t *q, int64_t m,
+                                unsigned long long *h) {
+  const int64_t t = blockIdx.x;
+  unsigned long long acc = 0;
+  for (int64_t j = threadIdx.x; j < m; j += blockDim.x)
+    acc += mix64((unsigned long long)load_any(tw, dtype, t * s0 + j * s1) ^ ((unsigned long long)j * 0x9E3779B97F4A7C15ull));
+  if (threadIdx.x == 0) acc += mix64((unsigned long long)q[t] + 0x5851F42D4C957F2Dull);
+  atomicAdd(&h[t], acc);
+}
+
+// rows whose hash matched their representative: compare every element
+__global__ void row_verify_kernel(const void *tw, int dtype, int64_t s0, int64_t s1, const int64_t *q, int64_t m,
+                                  const int32_t *rep, int *bad) {
+  const int64_t t = blockIdx.x;
+  const int64_t r = rep[t];
+  if (r == t) return;
+  if (q[t] != q[r]) {
+    if (threadIdx.x == 0) bad[t] = 1;
+    return;
+  }
+  for (int64_t j = threadIdx.x; j < m; j += blockDim.x)
+    if (load_any(tw, dtype, t * s0 + j * s1) != load_any(tw, dtype, r * s0 + j * s1)) bad[t] = 1;
 }
 
 int twiddle_table(const heal_tensor &tw, const heal_tensor &p, int wide, TwiddleTable *out) {
@@ -524,11 +559,77 @@ int twiddle_table(const heal_tensor &tw, const heal_tensor &p, int wide, Twiddle
   CacheEntry *e = cache_lookup(key);
   if (!e) {
     CacheEntry &n = cache_insert(key, {tw.data, p.data});
-    HEAL_CHECK(build_pairs(tw.data, tw.dtype, tw.strides[0], tw.strides[1], mi.q, tw.dims[0], tw.dims[1], wide, n));
+    const int64_t k = tw.dims[0], m = tw.dims[1];
+    // rows with equal content and modulus (tiled moduli, repeated
+    // ciphertext components) share one row of the Shoup table
+    std::vector<int32_t> rep(k);
+    for (int64_t t = 0; t < k; ++t) rep[t] = (int32_t)t;
+    if (k > 1 && m > 0) {
+      void *hb, *rb, *bb;
+      HEAL_CHECK(scratch_alloc(sizeof(unsigned long long) * k, &hb));
+      HEAL_TRY_CUDA(cudaMemsetAsync(hb, 0, sizeof(unsigned long long) * k, stream()));
+      row_hash_kernel<<<(unsigned)k, 256, 0, stream()>>>(tw.data, tw.dtype, tw.strides[0], tw.strides[1], mi.q, m,
+                                                       (unsigned long long *)hb);
+      HEAL_CHECK(check_launch("row_hash"));
+      std::vector<unsigned long long> hh(k);
+      HEAL_TRY_CUDA(cudaMemcpyAsync(hh.data(), hb, sizeof(unsigned long long) * k, cudaMemcpyDeviceToHost, stream()));
+      HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
+      scratch_free(hb);
+      std::unordered_map<unsigned long long, int32_t> first;
+      bool any = false;
+      for (int64_t t = 0; t < k; ++t) {
+        auto it = first.find(hh[t]);
+        if (it == first.end()) {
+          first[hh[t]] = (int32_t)t;
+        } else {
+          rep[t] = it->second;
+          any = true;
+        }
+      }
+      if (any) {
+        HEAL_CHECK(scratch_alloc(sizeof(int32_t) * k, &rb));
+        HEAL_CHECK(scratch_alloc(sizeof(int) * k, &bb));
+        HEAL_TRY_CUDA(cudaMemcpyAsync(rb, rep.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream()));
+        HEAL_TRY_CUDA(cudaMemsetAsync(bb, 0, sizeof(int) * k, stream()));
+        row_verify_kernel<<<(unsigned)k, 256, 0, stream()>>>(tw.data, tw.dtype, tw.strides[0], tw.strides[1], mi.q, m,
+                                                           (const int32_t *)rb, (int *)bb);
+        HEAL_CHECK(check_launch("row_verify"));
+        std::vector<int> bad(k);
+        HEAL_TRY_CUDA(cudaMemcpyAsync(bad.data(), bb, sizeof(int) * k, cudaMemcpyDeviceToHost, stream()));
+        HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
+        scratch_free(rb);
+        scratch_free(bb);
+        for (int64_t t = 0; t < k; ++t)
+          if (bad[t]) rep[t] = (int32_t)t;
+      }
+    }
+    std::vector<int32_t> rows, rowmap(k);
+    std::vector<int32_t> compact(k, -1);
+    for (int64_t t = 0; t < k; ++t) {
+      if (rep[t] == t) {
+        compact[t] = (int32_t)rows.size();
+        rows.push_back((int32_t)t);
+      }
+    }
+    for (int64_t t = 0; t < k; ++t) rowmap[t] = compact[rep[t]];
+    void *rows_d, *map_d;
+    HEAL_CHECK(scratch_alloc(sizeof(int32_t) * std::max<size_t>(rows.size(), 1), &rows_d));
+    HEAL_CHECK(scratch_alloc(sizeof(int32_t) * std::max<int64_t>(k, 1), &map_d));
+    if (!rows.empty())
+      HEAL_TRY_CUDA(cudaMemcpyAsync(rows_d, rows.data(), sizeof(int32_t) * rows.size(), cudaMemcpyHostToDevice, stream()));
+    if (k) HEAL_TRY_CUDA(cudaMemcpyAsync(map_d, rowmap.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, stream()));
+    HEAL_CHECK(build_pairs(tw.data, tw.dtype, tw.strides[0], tw.strides[1], mi.q, (const int32_t *)rows_d,
+                           (int64_t)rows.size(), m, wide, n));
+    n.bufs.push_back(map_d);   // bufs: pairs, neg flag, rowmap
+    // the host vectors above must outlive the copies that read them
+    HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
+    scratch_free(rows_d);
+    n.i0 = (int64_t)rows.size();
     e = &n;
   }
   out->pairs = e->bufs[0];
   out->neg_flag = (const int *)e->bufs[1];
+  out->rowmap = (const int32_t *)e->bufs[2];
   out->wide = wide;
   return HEAL_OK;
 }
@@ -541,11 +642,12 @@ int minv_table(const heal_tensor &minv, const heal_tensor &p, int64_t k, int wid
   CacheEntry *e = cache_lookup(key);
   if (!e) {
     CacheEntry &n = cache_insert(key, {minv.data, p.data});
-    HEAL_CHECK(build_pairs(minv.data, minv.dtype, minv.strides[0], 0, mi.q, k, 1, wide, n));
+    HEAL_CHECK(build_pairs(minv.data, minv.dtype, minv.strides[0], 0, mi.q, nullptr, k, 1, wide, n));
     e = &n;
   }
   out->pairs = e->bufs[0];
   out->neg_flag = (const int *)e->bufs[1];
+  out->rowmap = nullptr;
   out->wide = wide;
   return HEAL_OK;
 }

@@ -63,7 +63,8 @@ def _torch_paths():
 def build(verbose: bool = False, force: bool = False) -> dict:
     os.makedirs(OBJ, exist_ok=True)
     nvcc = _nvcc()
-    headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    headers = (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh"))
+               + glob.glob(os.path.join(ROOT, "include", "*.h")))
     api_headers = headers + glob.glob(os.path.join(CSRC, "lattica", "*.h"))
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     tinc, tlib, abi = _torch_paths()
@@ -78,7 +79,7 @@ def build(verbose: bool = False, force: bool = False) -> dict:
         cu_objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-c", src, "-o", obj])
+                         *os.environ.get("HEAL_NVCC_EXTRA", "").split(), "-c", src, "-o", obj])
     api_src = os.path.join(CSRC, "lattica", "lattica_api.cpp")
     api_obj = os.path.join(OBJ, "lattica_api.o")
     if force or _stale(api_obj, [api_src] + api_headers):

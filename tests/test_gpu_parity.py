@@ -291,3 +291,34 @@ def test_permute_and_axis_modsum_vs_oracle():
         got = run("heal_axis_modsum", up(np.ascontiguousarray(np.moveaxis(moved, 3, 4))).moveaxis(4, 3), p, 3,
                   out_shape=(2, 64, 1, 5), dtype=dt)
         assert np.array_equal(got, O.axis_modsum(moved, p, 3))
+
+
+@pytest.mark.parametrize("m", [256, 8192])
+def test_twiddle_rows_shared_only_when_equal(m):
+    # rows 0, 1, 3 equal; row 2 equal to row 0 except one element; row 4 has
+    # row 0's twiddles but another modulus: only truly equal rows may share
+    q0, q1 = P.ntt_primes(2**50, m, 2)
+    _, perm, tw, _, _ = P.ntt_tables([q0, q1], m)
+    base = tw[0]
+    rows = np.stack([base, base, base.copy(), base, base])
+    rows[2, m // 3] = (rows[2, m // 3] + 1) % q0
+    p = np.array([q0, q0, q0, q0, q1])
+    a = P.residues(31, (2, m, 1, 5), p)
+    assert np.array_equal(ntt(a, p, perm, rows), O.ntt(a, p, perm, rows))
+
+
+@pytest.mark.parametrize("dt,bits,power", [(np.int32, 40, 2), (np.int32, 32, 3), (np.int32, 7, 5),
+                                           (np.int64, 17, 3), (np.int64, 63, 2), (np.int64, 0, 2),
+                                           (np.int64, 9, 12)])
+def test_g_decomposition_vs_oracle(dt, bits, power):
+    lim = 2**31 if dt == np.int32 else 2**63
+    a = P.uniform(41, (3, 64, 1, 8), -lim // 2, lim // 2, dt)
+    a.flat[:4] = [0, -1, 1, -lim // 2]
+    want, _ = O.g_decomposition(a, power, bits)
+    got = run("heal_g_decomposition", a, power, bits, out_shape=a.shape + (power,), dtype=dt)
+    assert np.array_equal(got, want)
+    # a strided input takes the general kernel
+    v = np.ascontiguousarray(a.transpose(1, 0, 2, 3)).transpose(1, 0, 2, 3)
+    got = run("heal_g_decomposition", v, power, bits, out_shape=a.shape + (power,), dtype=dt)
+    assert np.array_equal(got, want)
+    capi.synchronize()
