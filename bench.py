@@ -290,6 +290,11 @@ def our_arm(args):
     capi.lib().heal_host_free(pin_in)
     capi.lib().heal_host_free(pin_out)
 
+    # ---- the other configurations (reported beside the headline)
+    configs = {}
+    if not args.skip_configs:
+        configs = other_configs(args, timed, stream)
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if world == 1 and not args.skip_cpu:
@@ -313,17 +318,61 @@ def our_arm(args):
                 "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
                 "gpu_launches": launches, "launches_per_step": launches / args.steps,
                 "split_ms": split_ms,
-                "clocks": clocks, "cpu_baseline": cpu}
+                "clocks": clocks, "cpu_baseline": cpu, "configs": configs}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
 
 
+def other_configs(args, timed, stream):
+    """cfg1 (plain and as one CUDA graph) and cfg4, timed like the headline."""
+    import hashlib
+    from heal_gb300 import capi
+    from heal_gb300.configs import Cfg1, Cfg4
+    out = {}
+    c1 = Cfg1()
+    c1.run()
+    with open(os.path.join(ROOT, "tests", "golden", "golden_hash.json")) as f:
+        gh = json.load(f)["cfg1"]
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a.numpy()).tobytes()).hexdigest()
+    exact = sha(c1.NA) == gh["ntt_a"] and sha(c1.AS) == gh["axis_modsum"] and sha(c1.RA) == gh["intt_ntt_a"]
+    steps = max(args.steps, 50)
+    for _ in range(3):
+        c1.run()
+    ms_plain, l_plain = timed(lambda s: c1.run(), steps)
+    graph = capi.Graph(c1.run)
+    for _ in range(3):
+        graph.launch()
+    ms_graph, l_graph = timed(lambda s: graph.launch(), steps)
+    exact = exact and sha(c1.AS) == gh["axis_modsum"]
+    out["cfg1"] = {"workload": "ntt(A), ntt(B), intt(ntt(A)), modmul, axis_modsum over the batch; [8, 4096, 1, 4] "
+                               "int64, 30-bit primes", "bit_exact_vs_reference_hashes": exact,
+                   "step_us_plain": ms_plain / steps * 1e3, "step_us_graph": ms_graph / steps * 1e3,
+                   "transform_limbs_per_s_graph": c1.transform_limbs() * steps / (ms_graph / 1e3),
+                   "launches_per_step": l_graph / steps}
+    del graph
+    c4 = Cfg4()
+    c4.ntt()
+    c4.intt()
+    round_trip = bool(np.array_equal(c4.Z.numpy()[:2], c4.host_x[:2]))
+    st4 = max(10, args.steps // 10)
+    ms4, _ = timed(lambda s: c4.ntt(), st4)
+    ms4i, _ = timed(lambda s: c4.intt(), st4)
+    hbm, _ = peaks()
+    per = ms4 / st4
+    out["cfg4"] = {"workload": "ntt on [64, 65536, 1, 32] int32, 31-bit primes, radix-8 Shoup butterflies on the integer pipes",
+                   "ntt_ms": per, "intt_ms": ms4i / st4, "limbs_per_s": c4.limbs() / (per / 1e3),
+                   "hbm_frac": c4.bytes_per_call() / (per / 1e3) / 1e9 / hbm, "round_trip_exact": round_trip}
+    return out
+
+
 def ntt_probe(args):
-    """--mode ntt: the batched NTT alone on [batch, 65536, 1, 72] int64 (the
-    digit tensor of `batch` / 2 chains); used for ncu captures of the pass
-    kernels.  Prints one JSON line with the CUDA-event time per call."""
+    """--mode ntt: one batched NTT alone, for ncu captures of the pass
+    kernels.  --probe digits: [batch, 65536, 1, 72] int64 under the chain's
+    50-bit primes tiled 3x (the digit tensor of batch/2 chains); --probe cfg4:
+    [batch, 65536, 1, 32] int32 under 31-bit primes.  Prints one JSON line
+    with the CUDA-event time per call."""
     import torch
     import heal_gb300
     from heal_gb300 import capi
@@ -331,12 +380,17 @@ def ntt_probe(args):
     heal_gb300.build()
     capi.check(capi.lib().heal_init(0))
     stream = torch.cuda.ExternalStream(capi.stream())
-    qs = P.ntt_primes(1 << BOUND, N, L)
-    p, perm, tw, itw, minv = P.ntt_tables(qs, N)
-    p_t, tw_t = np.repeat(p, D), np.repeat(tw, D, axis=0)
-    shape = (args.batch, N, 1, L * D)
-    x = capi.DeviceArray.from_numpy(P.residues(3, shape, p_t))
-    y = capi.DeviceArray.empty(shape, np.int64)
+    if args.probe == "cfg4":
+        dt, k, qs = np.int32, 32, P.ntt_primes(1 << 31, N, 32)
+        p_t, perm, tw_t, itw, minv = P.ntt_tables(qs, N, dt)
+    else:
+        dt, k = np.int64, L * D
+        qs = P.ntt_primes(1 << BOUND, N, L)
+        p, perm, tw, itw, minv = P.ntt_tables(qs, N)
+        p_t, tw_t = np.repeat(p, D), np.repeat(tw, D, axis=0)
+    shape = (args.batch, N, 1, k)
+    x = capi.DeviceArray.from_numpy(P.residues(3, shape, p_t, dt))
+    y = capi.DeviceArray.empty(shape, dt)
     dev = [capi.DeviceArray.from_numpy(v) for v in (p_t, perm, tw_t)]
     call = lambda: capi.call("heal_ntt", x, dev[0], dev[1], dev[2], None, None, y)
     for _ in range(args.warmup):
@@ -349,9 +403,11 @@ def ntt_probe(args):
     stop.record(stream)
     stop.synchronize()
     ms = start.elapsed_time(stop) / args.steps
-    limbs = args.batch * L * D
-    print(json.dumps({"mode": "ntt", "shape": list(shape), "ms_per_call": ms, "limbs_per_s": limbs / (ms / 1e3),
-                      "algorithmic_GBps": 2 * limbs * N * 8 / (ms / 1e3) / 1e9}), flush=True)
+    limbs = args.batch * k
+    esz = np.dtype(dt).itemsize
+    print(json.dumps({"mode": "ntt", "probe": args.probe, "shape": list(shape), "ms_per_call": ms,
+                      "limbs_per_s": limbs / (ms / 1e3),
+                      "algorithmic_GBps": 2 * limbs * N * esz / (ms / 1e3) / 1e9}), flush=True)
     return 0
 
 
@@ -363,8 +419,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--mode", default="chain", choices=["chain", "ntt"])
     ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--probe", default="digits", choices=["digits", "cfg4"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

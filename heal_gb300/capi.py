@@ -35,6 +35,10 @@ SIGNATURES = {
     "heal_get_stream": ([], _VP),
     "heal_set_stream": ([_VP], ctypes.c_int),
     "heal_kernel_launch_count": ([], _U64),
+    "heal_graph_begin": ([], ctypes.c_int),
+    "heal_graph_end": ([ctypes.POINTER(_VP)], ctypes.c_int),
+    "heal_graph_launch": ([_VP], ctypes.c_int),
+    "heal_graph_destroy": ([_VP], ctypes.c_int),
     "heal_alloc": ([_SZ, ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
     "heal_free": ([_VP], ctypes.c_int),
     "heal_h2d": ([_VP, _VP, _SZ], ctypes.c_int),
@@ -242,3 +246,30 @@ def launches() -> int:
 
 def stream() -> int:
     return int(lib().heal_get_stream() or 0)
+
+
+class Graph:
+    """A captured sequence of C-ABI calls, replayed with one launch."""
+
+    def __init__(self, record):
+        """`record()` issues the calls to capture; run it once uncaptured
+        first so that every table it needs is cached."""
+        check(lib().heal_graph_begin())
+        try:
+            record()
+        except BaseException:
+            h = ctypes.c_void_p()
+            lib().heal_graph_end(ctypes.byref(h))
+            if h.value:
+                lib().heal_graph_destroy(h)
+            raise
+        self.handle = ctypes.c_void_p()
+        check(lib().heal_graph_end(ctypes.byref(self.handle)))
+
+    def launch(self):
+        check(lib().heal_graph_launch(self.handle))
+
+    def __del__(self):
+        if getattr(self, "handle", None) is not None and self.handle.value and _lib is not None:
+            _lib.heal_graph_destroy(self.handle)
+            self.handle = ctypes.c_void_p()

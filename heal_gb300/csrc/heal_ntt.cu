@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -158,7 +159,15 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   // moduli >= 2^62 do not fit the 64-bit lazy ranges
   base.force_exact = m == 1 || mi.max_q >= (int64_t(1) << 62);
   const bool is32 = dt == HEAL_INT32;
-  int C = 8;
+  // limbs per tile: 4 measured best for both int32 and int64 (more, smaller
+  // CTAs; fewer threads per barrier).  Neighbouring CTAs take neighbouring
+  // limb groups, so a DRAM sector shared by two tiles is read once into L2
+  static const int kTileLimbsEnv = [] {
+    const char *e = getenv("HEAL_NTT_TILE_LIMBS");
+    int v = e ? atoi(e) : 0;
+    return (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) ? v : 0;
+  }();
+  int C = kTileLimbsEnv ? kTileLimbsEnv : 4;
   while (C > 1 && C / 2 >= k) C /= 2;
   int rc = HEAL_OK;
   void *tmp = nullptr, *tmp2 = nullptr;

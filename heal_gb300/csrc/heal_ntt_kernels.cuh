@@ -126,14 +126,16 @@ __device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
   x.P = 1 << g.p;
   x.C = g.C;
   x.logC = g.logC;
-  // (i, j) vary fastest: the CTAs that read the same twiddle rows (same
-  // limbs, same set) run back to back and share them through L2
+  // Limb groups vary fastest, then (i, j), then the set: neighbouring row
+  // segments of one set are read back to back (one DRAM line serves them
+  // all), and the CTAs that share twiddle rows (same set and limbs, other
+  // i, j) run within a window of ngroups_t * l * r blocks.
   const int64_t bid = blockIdx.x;
   const int64_t nij = g.l * g.r;
-  const int64_t ij = bid % nij;
-  const int64_t rest = bid / nij;
-  x.rset = rest % g.nsets;
-  const int64_t tg = rest / g.nsets;
+  const int64_t tg = bid % g.ngroups_t;
+  const int64_t rest = bid / g.ngroups_t;
+  const int64_t ij = rest % nij;
+  x.rset = rest / nij;
   x.j = ij % g.r;
   x.i = ij / g.r;
   x.t0 = tg * g.C;
@@ -416,11 +418,14 @@ __device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::
   constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
   if constexpr (STEP < NSTEP) {
     if constexpr (STEP > 0) {
+      // the fast path exchanges words of its own width (4 bytes in the
+      // 32-bit modes); the exact path never shares a CTA with it
+      W *wt = reinterpret_cast<W *>(tile);
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP>(STEP - 1, r, e), c, logC)] = (int64_t)v[e];
+      for (int e = 0; e < kPT; ++e) wt[tidx(point_of<INV, LOGP>(STEP - 1, r, e), c, logC)] = v[e];
       __syncthreads();
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) v[e] = (W)tile[tidx(point_of<INV, LOGP>(STEP, r, e), c, logC)];
+      for (int e = 0; e < kPT; ++e) v[e] = wt[tidx(point_of<INV, LOGP>(STEP, r, e), c, logC)];
       __syncthreads();
     }
     reg_step<MODE, INV, LOGP, STEP>(v, r, G, twp, q);
@@ -445,14 +450,28 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
   const int64_t tq = act ? t : g.k - 1;
   const int64_t q64 = g.q[tq];
 
-  // ---- load (step-0 layout)
+  // ---- load (step-0 layout).  In the first and the last step a thread's
+  // points sit at offsets point_of(step, 0, e) from its first point, the
+  // same for every thread, so one base pointer and one row stride address
+  // them all.
+  const int64_t rowmul = g.kind == KIND_BLOCK ? 1 : g.nsets;
   int64_t raw[kPT];
   int neg = 0;
+  if (g.load_map) {
 #pragma unroll
-  for (int e = 0; e < kPT; ++e) {
-    const int s = point_of<INV, LOGP>(0, r, e);
-    raw[e] = act ? load_point<T>(g, x, s, t) : 0;
-    neg |= needs_exact<INV>(g, raw[e], q64);
+    for (int e = 0; e < kPT; ++e) {
+      raw[e] = act ? load_point<T>(g, x, point_of<INV, LOGP>(0, r, e), t) : 0;
+      neg |= needs_exact<INV>(g, raw[e], q64);
+    }
+  } else {
+    const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + tq * g.ss[3]) +
+                  x.row_of(g, point_of<INV, LOGP>(0, r, 0)) * g.ss[1];
+    const int64_t rs = rowmul * g.ss[1];
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      raw[e] = act ? (int64_t)p0[point_of<INV, LOGP>(0, 0, e) * rs] : 0;
+      neg |= needs_exact<INV>(g, raw[e], q64);
+    }
   }
   const bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
                      (g.scale && g.minv_neg && *g.minv_neg);
@@ -487,14 +506,16 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
 
   // ---- store
   if (g.store_gather) {  // single-pass forward: out[u] = res[perm[u]]
+    W *wt = reinterpret_cast<W *>(tile);
+    if (NSTEP == 1) __syncthreads();  // no exchange ran: the tile may still hold raw loads
 #pragma unroll
-    for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP>(NSTEP - 1, r, e), c, logC)] = (int64_t)v[e];
+    for (int e = 0; e < kPT; ++e) wt[tidx(point_of<INV, LOGP>(NSTEP - 1, r, e), c, logC)] = v[e];
     __syncthreads();
     if (act) {
 #pragma unroll
       for (int e = 0; e < kPT; ++e) {
         const int s = point_of<INV, LOGP>(0, r, e);
-        store_point<T>(g, x, s, t, tile[tidx(g.store_gather[s], c, logC)]);
+        store_point<T>(g, x, s, t, (int64_t)wt[tidx(g.store_gather[s], c, logC)]);
       }
     }
     return;
@@ -502,11 +523,23 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
   if (!act) return;
   Pair mp;
   if (g.scale) mp = __ldg((const Pair *)g.minv_pairs + t);
+  if (g.store_scatter) {
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      W val = v[e];
+      if (g.scale) val = mulw<WIDE>(val, mp, q);
+      store_point<T>(g, x, point_of<INV, LOGP>(NSTEP - 1, r, e), t, (int64_t)val);
+    }
+    return;
+  }
+  T *p1 = (T *)g.dst + (x.i * g.ds[0] + x.j * g.ds[2] + t * g.ds[3]) +
+          x.row_of(g, point_of<INV, LOGP>(NSTEP - 1, r, 0)) * g.ds[1];
+  const int64_t rsd = rowmul * g.ds[1];
 #pragma unroll
   for (int e = 0; e < kPT; ++e) {
     W val = v[e];
     if (g.scale) val = mulw<WIDE>(val, mp, q);
-    store_point<T>(g, x, point_of<INV, LOGP>(NSTEP - 1, r, e), t, (int64_t)val);
+    p1[point_of<INV, LOGP>(NSTEP - 1, 0, e) * rsd] = (T)(int64_t)val;
   }
 }
 

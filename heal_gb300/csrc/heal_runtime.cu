@@ -40,6 +40,8 @@ int cuda_fail(cudaError_t e, const char *what) {
 // ================================================================= runtime
 struct Runtime {
   bool ready = false;
+  bool capturing = false;
+  uint64_t capture_start = 0;  // launch count when the capture began
   int device = -1;
   int sms = 0;
   cudaStream_t own = nullptr;
@@ -312,7 +314,14 @@ static void drop_entry(CacheEntry &e) {
   e.bufs.clear();
 }
 
-// Returns the valid entry for `key`, or nullptr (after dropping a stale one).
+static int refuse_in_capture(const char *what) {
+  return set_error(HEAL_ERR_RUNTIME, std::string(what) +
+                                         ": the table for this tensor is not cached yet; run the call once before "
+                                         "capturing it in a graph");
+}
+
+// Returns the valid entry for `key`, or nullptr (after dropping a stale one;
+// while a graph is being captured a stale entry is left alone).
 static CacheEntry *cache_lookup(const std::string &key) {
   auto it = g_cache.find(key);
   if (it == g_cache.end()) return nullptr;
@@ -322,6 +331,7 @@ static CacheEntry *cache_lookup(const std::string &key) {
     if (g != d.second || (g == 0 && it->second.epoch != g_epoch.load())) ok = false;
   }
   if (!ok) {
+    if (g_rt.capturing) return nullptr;
     drop_entry(it->second);
     g_cache.erase(it);
     return nullptr;
@@ -395,6 +405,7 @@ int mod_table(const heal_tensor &p, ModTable *out) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   std::string key = key_of("mod", {&p});
   CacheEntry *e = cache_lookup(key);
+  if (!e && g_rt.capturing) return refuse_in_capture("modulus constants");
   if (!e) {
     CacheEntry &n = cache_insert(key, {p.data});
     int64_t cnt = numel(p);
@@ -433,6 +444,7 @@ int mod_info(const heal_tensor &p, ModInfo *out) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   std::string key = key_of("modinfo", {&p});
   CacheEntry *e = cache_lookup(key);
+  if (!e && g_rt.capturing) return refuse_in_capture("mod_info");
   if (!e) {
     CacheEntry &n = cache_insert(key, {p.data});
     int64_t k = p.ndim ? p.dims[0] : 1;
@@ -557,6 +569,7 @@ int twiddle_table(const heal_tensor &tw, const heal_tensor &p, int wide, Twiddle
   HEAL_CHECK(mod_info(p, &mi));
   std::string key = key_of("tw", {&tw, &p}, wide);
   CacheEntry *e = cache_lookup(key);
+  if (!e && g_rt.capturing) return refuse_in_capture("twiddle table");
   if (!e) {
     CacheEntry &n = cache_insert(key, {tw.data, p.data});
     const int64_t k = tw.dims[0], m = tw.dims[1];
@@ -676,6 +689,7 @@ int perm_info(const heal_tensor &perm, PermInfo *out) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   std::string key = key_of("perm", {&perm});
   CacheEntry *e = cache_lookup(key);
+  if (!e && g_rt.capturing) return refuse_in_capture("permutation table");
   if (!e) {
     CacheEntry &n = cache_insert(key, {perm.data});
     int64_t m = perm.dims[0];
@@ -722,6 +736,7 @@ int perms_valid(const heal_tensor &perms, int64_t m, bool *ok) {
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   std::string key = key_of("perms", {&perms}, m);
   CacheEntry *e = cache_lookup(key);
+  if (!e && g_rt.capturing) return refuse_in_capture("permutation check");
   if (!e) {
     CacheEntry &n = cache_insert(key, {perms.data});
     void *cnt;
@@ -758,6 +773,55 @@ int heal_init(int device) {
 }
 
 const char *heal_last_error(void) { return g_last_error.c_str(); }
+
+struct HealGraph {
+  cudaGraphExec_t exec;
+  uint64_t kernels;  // kernel launches recorded in the graph
+};
+
+int heal_graph_begin(void) {
+  clear_error();
+  HEAL_CHECK(ensure_init());
+  if (g_rt.capturing) return set_error(HEAL_ERR_RUNTIME, "heal_graph_begin: already capturing");
+  HEAL_TRY_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal));
+  g_rt.capturing = true;
+  g_rt.capture_start = g_rt.launches.load();
+  return HEAL_OK;
+}
+
+int heal_graph_end(void **graph) {
+  clear_error();
+  if (!graph) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_graph_end: graph must not be null");
+  *graph = nullptr;
+  if (!g_rt.capturing) return set_error(HEAL_ERR_RUNTIME, "heal_graph_end: not capturing");
+  g_rt.capturing = false;
+  cudaGraph_t g = nullptr;
+  const uint64_t recorded = g_rt.launches.load() - g_rt.capture_start;
+  g_rt.launches.fetch_sub(recorded);  // counted again at every replay
+  HEAL_TRY_CUDA(cudaStreamEndCapture(stream(), &g));
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  *graph = new HealGraph{exec, recorded};
+  return HEAL_OK;
+}
+
+int heal_graph_launch(void *graph) {
+  if (!graph) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_graph_launch: graph must not be null");
+  HealGraph *hg = (HealGraph *)graph;
+  HEAL_TRY_CUDA(cudaGraphLaunch(hg->exec, stream()));
+  note_launch((int)hg->kernels);
+  return HEAL_OK;
+}
+
+int heal_graph_destroy(void *graph) {
+  if (!graph) return HEAL_OK;
+  HealGraph *hg = (HealGraph *)graph;
+  cudaGraphExecDestroy(hg->exec);
+  delete hg;
+  return HEAL_OK;
+}
 
 int heal_synchronize(void) {
   HEAL_CHECK(ensure_init());

@@ -86,8 +86,21 @@ void *heal_get_stream(void);
  * library's own stream). */
 int heal_set_stream(void *stream);
 
-/* Number of kernels this library has launched since heal_init. */
+/* Number of kernels this library has launched since heal_init (a graph
+ * replay counts the kernels it contains). */
 uint64_t heal_kernel_launch_count(void);
+
+/* CUDA graphs of HEAL calls.  heal_graph_begin starts capturing the library
+ * stream; every compute call until heal_graph_end is recorded instead of run,
+ * and heal_graph_end returns an instantiated graph that heal_graph_launch
+ * replays on the library stream.  The tables the recorded calls derive from
+ * their inputs must already be cached (run each call once before capturing);
+ * a call that would have to build one fails during capture.  No counterpart
+ * in HEAL: a way to issue a fixed sequence of calls with one launch. */
+int heal_graph_begin(void);
+int heal_graph_end(void **graph);
+int heal_graph_launch(void *graph);
+int heal_graph_destroy(void *graph);
 
 /* ------------------------------------------- device memory (HBM residency)
  * Replaces allocate_on_hardware / host_to_device / device_to_host

@@ -322,3 +322,15 @@ def test_g_decomposition_vs_oracle(dt, bits, power):
     got = run("heal_g_decomposition", v, power, bits, out_shape=a.shape + (power,), dtype=dt)
     assert np.array_equal(got, want)
     capi.synchronize()
+
+
+def test_cfg4_int32_31bit_columns_vs_oracle():
+    # int32 residues under 31-bit primes: the reference's int32 NTT overflows
+    # u + q - v here, so the oracle runs in its exact mode (double width)
+    m, k = 65536, 4
+    qs = P.ntt_primes(2**31, m, k)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m, np.int32)
+    a = P.residues(77, (2, m, 1, k), qs, np.int32)
+    fw = ntt(a, p, perm, tw)
+    assert np.array_equal(fw, O.ntt(a, p, perm, tw, exact=1))
+    assert np.array_equal(intt(fw, p, perm, itw, minv), a)
