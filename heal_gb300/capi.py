@@ -39,6 +39,8 @@ SIGNATURES = {
     "heal_graph_end": ([ctypes.POINTER(_VP)], ctypes.c_int),
     "heal_graph_launch": ([_VP], ctypes.c_int),
     "heal_graph_destroy": ([_VP], ctypes.c_int),
+    "heal_graph_fork": ([ctypes.c_int], ctypes.c_int),
+    "heal_graph_branch": ([ctypes.c_int], ctypes.c_int),
     "heal_alloc": ([_SZ, ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
     "heal_free": ([_VP], ctypes.c_int),
     "heal_h2d": ([_VP, _VP, _SZ], ctypes.c_int),
@@ -76,6 +78,12 @@ SIGNATURES = {
     "heal_ntt": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "heal_intt": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "heal_permute": ([_P, _P, _P, _I64, _I64], ctypes.c_int),
+    "heal_ntt_set_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "heal_ntt_get_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.POINTER(ctypes.c_int),
+                           ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "heal_ntt_clear_plans": ([], ctypes.c_int),
+    "heal_ntt_autotune": ([ctypes.c_int, _P, _P, _P, _P, _P, _P, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                           ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
 }
 
 
@@ -251,12 +259,19 @@ def stream() -> int:
 class Graph:
     """A captured sequence of C-ABI calls, replayed with one launch."""
 
-    def __init__(self, record):
+    def __init__(self, record, branches: int = 0):
         """`record()` issues the calls to capture; run it once uncaptured
-        first so that every table it needs is cached."""
+        first so that every table it needs is cached.  With `branches` > 0
+        the capture forks that many parallel branch streams first and
+        `record(branch)` gets a function that sends the following calls to
+        branch i (-1: the capture's own stream)."""
         check(lib().heal_graph_begin())
         try:
-            record()
+            if branches:
+                check(lib().heal_graph_fork(branches))
+                record(lambda i: check(lib().heal_graph_branch(i)))
+            else:
+                record()
         except BaseException:
             h = ctypes.c_void_p()
             lib().heal_graph_end(ctypes.byref(h))
@@ -273,3 +288,18 @@ class Graph:
         if getattr(self, "handle", None) is not None and self.handle.value and _lib is not None:
             _lib.heal_graph_destroy(self.handle)
             self.handle = ctypes.c_void_p()
+
+
+def autotune_ntt(inverse: bool, a, p, perm, tw, minv, out, reps: int = 5) -> tuple[int, int]:
+    """Runs heal_ntt_autotune on these operands (`out` is overwritten) and
+    returns the chosen (tile_limbs, first_pass_log2)."""
+    c, s = ctypes.c_int(), ctypes.c_int()
+    check(lib().heal_ntt_autotune(int(inverse), _arg(a), _arg(p), _arg(perm), _arg(tw), _arg(minv), _arg(out),
+                                  reps, ctypes.byref(c), ctypes.byref(s)))
+    return c.value, s.value
+
+
+def ntt_plan(dtype, inverse: bool, m: int, k: int) -> tuple[int, int]:
+    c, s = ctypes.c_int(), ctypes.c_int()
+    check(lib().heal_ntt_get_plan(DTYPES[np.dtype(dtype)], int(inverse), m, k, ctypes.byref(c), ctypes.byref(s)))
+    return c.value, s.value

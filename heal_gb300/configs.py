@@ -75,3 +75,110 @@ class Cfg4:
 
     def bytes_per_call(self) -> int:
         return 2 * self.batch * self.N * self.L * 4
+
+
+class Cfg3:
+    """Ragged batch: `count` ciphertexts [2, N_i, 1, L_i] int64 with N_i drawn
+    from 2^logns and L_i uniform in 2..32, under the largest 30-bit primes
+    q = 1 (mod 2 N_i) (limb t of every ciphertext of ring degree N uses the
+    t-th such prime).  Every ciphertext runs the cfg1 chain: ntt(A_i),
+    ntt(B_i), intt(ntt(A_i)), modmul of the two NTTs, axis_modsum over the
+    polynomial axis.  The batch runs as a plain loop of C-ABI calls or as one
+    CUDA graph whose branches take the ciphertexts in parallel."""
+
+    COUNT, LOGNS, LMIN, LMAX, BOUND = 256, (12, 13, 14, 15, 16), 2, 32, 1 << 30
+
+    def __init__(self, count: int = COUNT, logns=LOGNS, seed: int = 303):
+        idx = P.uniform(seed, (count,), 0, len(logns))
+        ls = P.uniform(seed + 1, (count,), self.LMIN, self.LMAX + 1)
+        self.specs = [(1 << int(logns[i]), int(l)) for i, l in zip(idx, ls)]
+        D, E = capi.DeviceArray.from_numpy, capi.DeviceArray.empty
+        self.qs, self.tables = {}, {}
+        for n in sorted({n for n, _ in self.specs}):
+            qs = P.ntt_primes(self.BOUND, n, self.LMAX)
+            p, perm, tw, itw, minv = P.ntt_tables(qs, n)
+            self.qs[n] = qs
+            self.tables[n] = {"p": D(p), "perm": D(perm), "tw": D(tw), "itw": D(itw), "minv": D(minv)}
+        self.A, self.B, self.NA, self.NB, self.RA, self.PR, self.AS, self.views = ([] for _ in range(8))
+        for i, (n, l) in enumerate(self.specs):
+            shape = (2, n, 1, l)
+            self.A.append(D(P.residues(seed * 1000 + 2 * i, shape, self.qs[n][:l])))
+            self.B.append(D(P.residues(seed * 1000 + 2 * i + 1, shape, self.qs[n][:l])))
+            for lst in (self.NA, self.NB, self.RA, self.PR):
+                lst.append(E(shape, np.int64, zero=False))
+            self.AS.append(E((n, 1, l), np.int64, zero=False))
+            t = self.tables[n]
+            self.views.append({
+                "p": capi.DeviceArray(t["p"].buf, np.int64, (l,), (1,)),
+                "perm": t["perm"],
+                "tw": capi.DeviceArray(t["tw"].buf, np.int64, (l, n), (n, 1)),
+                "itw": capi.DeviceArray(t["itw"].buf, np.int64, (l, n), (n, 1)),
+                "minv": capi.DeviceArray(t["minv"].buf, np.int64, (l,), (1,)),
+            })
+
+    # ---- the chain of one ciphertext: five C-ABI calls
+    def chain(self, i: int):
+        v = self.views[i]
+        capi.call("heal_ntt", self.A[i], v["p"], v["perm"], v["tw"], None, None, self.NA[i])
+        capi.call("heal_ntt", self.B[i], v["p"], v["perm"], v["tw"], None, None, self.NB[i])
+        capi.call("heal_intt", self.NA[i], v["p"], v["perm"], v["itw"], v["minv"], None, None, self.RA[i])
+        capi.call("heal_modmul_ttt", self.NA[i], self.NB[i], v["p"], self.PR[i])
+        capi.call("heal_axis_modsum", self.PR[i], v["p"], self.AS[i], 0)
+
+    def run(self):
+        for i in range(len(self.specs)):
+            self.chain(i)
+
+    def schedule(self, branches: int) -> list[list[int]]:
+        """Ciphertexts per branch: largest first onto the least loaded branch."""
+        load, out = [0] * branches, [[] for _ in range(branches)]
+        for i in sorted(range(len(self.specs)), key=lambda i: -self.work(i)):
+            b = load.index(min(load))
+            out[b].append(i)
+            load[b] += self.work(i)
+        return out
+
+    def record(self, branches: int):
+        """Issues the batch for capture: branch b runs its ciphertexts in order."""
+        plan = self.schedule(branches)
+
+        def rec(branch):
+            for b, cts in enumerate(plan):
+                branch(b)
+                for i in cts:
+                    self.chain(i)
+            branch(-1)
+        return rec
+
+    def graph(self, branches: int = 16) -> capi.Graph:
+        return capi.Graph(self.record(branches), branches=branches)
+
+    def autotune(self, reps: int = 3) -> dict:
+        """Tunes the NTT plan of every distinct (N, L) shape of the batch,
+        forward and inverse; returns {(N, L): (forward plan, inverse plan)}."""
+        done = {}
+        for i, (n, l) in enumerate(self.specs):
+            if (n, l) in done:
+                continue
+            v = self.views[i]
+            fwd = capi.autotune_ntt(False, self.A[i], v["p"], v["perm"], v["tw"], None, self.NA[i], reps)
+            inv = capi.autotune_ntt(True, self.NA[i], v["p"], v["perm"], v["itw"], v["minv"], self.RA[i], reps)
+            done[(n, l)] = (fwd, inv)
+        return done
+
+    # ---- sizes
+    def work(self, i: int) -> int:
+        n, l = self.specs[i]
+        return n.bit_length() * n * l
+
+    def elements(self) -> int:
+        return sum(2 * n * l for n, l in self.specs)
+
+    def transform_limbs(self) -> int:
+        return sum(3 * 2 * l for _, l in self.specs)
+
+    def bytes_per_step(self) -> int:
+        """Algorithmic bytes of one pass over the batch: three transforms (read
+        + write), modmul (two reads, one write), axis_modsum (read of both
+        polynomials, write of one)."""
+        return sum(2 * n * l * 8 * (2 + 2 + 2 + 3) + (2 * n * l + n * l) * 8 for n, l in self.specs)

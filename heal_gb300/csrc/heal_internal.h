@@ -30,6 +30,7 @@ void clear_error();
 // ----------------------------------------------------------------- runtime
 int ensure_init();
 cudaStream_t stream();
+bool capturing();  // a graph capture is open
 int device_sm_count();
 void note_launch(int n = 1);
 // checks the launch that was just enqueued

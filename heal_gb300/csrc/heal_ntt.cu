@@ -32,7 +32,11 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "heal_internal.h"
 #include "heal_ntt_kernels.cuh"
@@ -77,6 +81,47 @@ static int ilog2(int64_t x) {
   int r = 0;
   while ((int64_t(1) << r) < x) ++r;
   return r;
+}
+
+// --------------------------------------------------------------- plans
+// A plan fixes the limbs per tile and where the network splits into two
+// passes (first_log = log2 of the first pass's length; 0 = one pass).
+struct NttPlan {
+  int tile_limbs;
+  int first_log;
+};
+using PlanKey = std::tuple<int, int, int, int64_t>;  // dtype, inverse, log2 m, k
+static std::mutex g_plan_mu;
+static std::map<PlanKey, NttPlan> g_plans;
+
+static int default_tile_limbs() {
+  // 4 limbs per tile measured best for int32 and int64 alike (more, smaller
+  // CTAs; fewer threads per barrier).  Neighbouring CTAs take neighbouring
+  // limb groups, so a DRAM sector shared by two tiles is read once into L2.
+  static const int v = [] {
+    const char *e = getenv("HEAL_NTT_TILE_LIMBS");
+    int x = e ? atoi(e) : 4;
+    return (x == 1 || x == 2 || x == 4 || x == 8 || x == 16) ? x : 4;
+  }();
+  return v;
+}
+
+static NttPlan default_plan(int logm) {
+  return NttPlan{default_tile_limbs(), logm <= kSinglePassLogMax ? 0 : logm / 2};
+}
+
+static NttPlan plan_for(int dt, bool inv, int logm, int64_t k) {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  auto it = g_plans.find(PlanKey{dt, inv ? 1 : 0, logm, k});
+  return it != g_plans.end() ? it->second : default_plan(logm);
+}
+
+static bool plan_valid(const NttPlan &pl, int logm) {
+  const int c = pl.tile_limbs;
+  if (c < 1 || c > 16 || (c & (c - 1))) return false;
+  if (pl.first_log == 0) return logm <= kSinglePassLogMax;
+  const int second = logm - pl.first_log;
+  return pl.first_log >= 1 && pl.first_log <= kSinglePassLogMax && second >= 1 && second <= kSinglePassLogMax;
 }
 
 static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm,
@@ -159,15 +204,8 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   // moduli >= 2^62 do not fit the 64-bit lazy ranges
   base.force_exact = m == 1 || mi.max_q >= (int64_t(1) << 62);
   const bool is32 = dt == HEAL_INT32;
-  // limbs per tile: 4 measured best for both int32 and int64 (more, smaller
-  // CTAs; fewer threads per barrier).  Neighbouring CTAs take neighbouring
-  // limb groups, so a DRAM sector shared by two tiles is read once into L2
-  static const int kTileLimbsEnv = [] {
-    const char *e = getenv("HEAL_NTT_TILE_LIMBS");
-    int v = e ? atoi(e) : 0;
-    return (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) ? v : 0;
-  }();
-  int C = kTileLimbsEnv ? kTileLimbsEnv : 4;
+  const NttPlan plan = plan_for(dt, inv, logm, k);
+  int C = plan.tile_limbs;
   while (C > 1 && C / 2 >= k) C /= 2;
   int rc = HEAL_OK;
   void *tmp = nullptr, *tmp2 = nullptr;
@@ -185,7 +223,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
     return x.nsets * l * r * x.ngroups_t;
   };
 
-  if (logm <= kSinglePassLogMax) {
+  if (plan.first_log == 0) {
     NttArgs x = base;
     int64_t nb = cfg(x, logm, KIND_BLOCK);
     x.src = A.data;
@@ -204,7 +242,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
     rc = launch_any(x, nb, is32, mode, inv);
   } else {
     // two passes through a dense [l, m, r, k] scratch tensor
-    const int p1 = logm / 2, p2 = logm - p1;
+    const int p1 = plan.first_log, p2 = logm - p1;
     heal_tensor T1 = *res;
     int64_t s = 1;
     for (int d = 3; d >= 0; --d) {
@@ -305,6 +343,127 @@ int heal_intt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *per
   (void)log2p;
   (void)mu;
   return ntt_run(true, a, p, perm, inv_twiddles, m_inv, result);
+}
+
+static int plan_shape(int dtype, int inverse, int64_t m, int64_t k, int *logm) {
+  if (dtype != HEAL_INT32 && dtype != HEAL_INT64)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT plan: dtype must be HEAL_INT32 or HEAL_INT64");
+  if (inverse != 0 && inverse != 1) return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT plan: inverse must be 0 or 1");
+  if (m < 1 || (m & (m - 1)) || m > (int64_t(1) << (2 * kSinglePassLogMax)))
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT plan: m must be a power of two up to 2^24");
+  if (k < 1) return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT plan: k must be positive");
+  *logm = ilog2(m);
+  return HEAL_OK;
+}
+
+int heal_ntt_set_plan(int dtype, int inverse, int64_t m, int64_t k, int tile_limbs, int first_pass_log2) {
+  clear_error();
+  int logm;
+  HEAL_CHECK(plan_shape(dtype, inverse, m, k, &logm));
+  const NttPlan pl{tile_limbs, first_pass_log2};
+  if (!plan_valid(pl, logm))
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_ntt_set_plan: tile_limbs must be 1, 2, 4, 8 or 16 and "
+                                                "both passes 1..12 stages long (0 = one pass, m <= 4096)");
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  g_plans[PlanKey{dtype, inverse, logm, k}] = pl;
+  return HEAL_OK;
+}
+
+int heal_ntt_get_plan(int dtype, int inverse, int64_t m, int64_t k, int *tile_limbs, int *first_pass_log2) {
+  clear_error();
+  int logm;
+  HEAL_CHECK(plan_shape(dtype, inverse, m, k, &logm));
+  const NttPlan pl = plan_for(dtype, inverse != 0, logm, k);
+  if (tile_limbs) *tile_limbs = pl.tile_limbs;
+  if (first_pass_log2) *first_pass_log2 = pl.first_log;
+  return HEAL_OK;
+}
+
+int heal_ntt_clear_plans(void) {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  g_plans.clear();
+  return HEAL_OK;
+}
+
+int heal_ntt_autotune(int inverse, const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm,
+                      const heal_tensor *twiddles, const heal_tensor *m_inv, const heal_tensor *result, int reps,
+                      int *tile_limbs, int *first_pass_log2) {
+  clear_error();
+  HEAL_CHECK(ensure_init());
+  if (capturing()) return set_error(HEAL_ERR_RUNTIME, "heal_ntt_autotune: not allowed while a graph is being captured");
+  if (reps < 1) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_ntt_autotune: reps must be positive");
+  const bool inv = inverse != 0;
+  auto run = [&]() { return ntt_run(inv, a, p, perm, twiddles, inv ? m_inv : nullptr, result); };
+  HEAL_CHECK(run());  // validates the operands and caches their tables
+  const int dt = a->dtype;
+  const int64_t m = a->dims[1], k = a->dims[3];
+  if (m == 0 || a->dims[0] * a->dims[2] * k == 0) return HEAL_OK;
+  const int logm = ilog2(m);
+  const PlanKey key{dt, inv ? 1 : 0, logm, k};
+  NttPlan before;
+  bool had;
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_plans.find(key);
+    had = it != g_plans.end();
+    if (had) before = it->second;
+  }
+  // candidates: every distinct tile width, and the splits near the middle
+  std::vector<NttPlan> cands;
+  std::vector<int> splits;
+  if (logm <= kSinglePassLogMax) splits.push_back(0);
+  if (logm >= 8)
+    for (int s = logm / 2 - 1; s <= logm / 2 + 1; ++s)
+      if (s >= 4 && logm - s >= 4 && s <= kSinglePassLogMax && logm - s <= kSinglePassLogMax) splits.push_back(s);
+  if (splits.empty()) splits.push_back(default_plan(logm).first_log);
+  for (int c = 1; c <= 16; c *= 2) {
+    if (c / 2 >= k) break;  // wider tiles shrink to this one
+    for (int s : splits) cands.push_back(NttPlan{c, s});
+  }
+  cudaEvent_t e0, e1;
+  HEAL_TRY_CUDA(cudaEventCreate(&e0));
+  HEAL_TRY_CUDA(cudaEventCreate(&e1));
+  int rc = HEAL_OK;
+  float best_ms = 0.f;
+  NttPlan best = default_plan(logm);
+  for (const NttPlan &pl : cands) {
+    {
+      std::lock_guard<std::mutex> lk(g_plan_mu);
+      g_plans[key] = pl;
+    }
+    rc = run();  // warm-up of this plan
+    if (rc) break;
+    cudaEventRecord(e0, stream());
+    for (int i = 0; i < reps && !rc; ++i) rc = run();
+    cudaEventRecord(e1, stream());
+    if (rc) break;
+    cudaError_t ce = cudaEventSynchronize(e1);
+    if (ce != cudaSuccess) {
+      rc = cuda_fail(ce, "heal_ntt_autotune");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (best_ms == 0.f || ms < best_ms) {
+      best_ms = ms;
+      best = pl;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (rc) {
+      if (had) g_plans[key] = before;
+      else g_plans.erase(key);
+    } else {
+      g_plans[key] = best;
+    }
+  }
+  if (rc) return rc;
+  if (tile_limbs) *tile_limbs = best.tile_limbs;
+  if (first_pass_log2) *first_pass_log2 = best.first_log;
+  return HEAL_OK;
 }
 
 }  // extern "C"

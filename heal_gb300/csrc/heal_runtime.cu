@@ -42,6 +42,10 @@ struct Runtime {
   bool ready = false;
   bool capturing = false;
   uint64_t capture_start = 0;  // launch count when the capture began
+  cudaStream_t origin = nullptr;         // the stream the capture began on
+  std::vector<cudaStream_t> branches;    // branch streams, kept for reuse
+  int forked = 0;                        // branches joined to this capture
+  cudaEvent_t join = nullptr;
   int device = -1;
   int sms = 0;
   cudaStream_t own = nullptr;
@@ -98,6 +102,8 @@ int check_launch(const char *what) {
   note_launch();
   return HEAL_OK;
 }
+
+bool capturing() { return g_rt.capturing; }
 
 int scratch_alloc(size_t bytes, void **out) {
   *out = nullptr;
@@ -292,7 +298,10 @@ struct CacheEntry {
 };
 static std::unordered_map<std::string, CacheEntry> g_cache;
 static uint64_t g_cache_clock = 0;
-constexpr size_t kCacheMax = 512;
+// A ragged batch touches five tables per distinct (m, k) shape (moduli
+// constants, moduli summary, twiddles, inverse twiddles, m_inv): 4096 entries
+// keep every shape of a few hundred ciphertexts resident for graph capture.
+constexpr size_t kCacheMax = 4096;
 
 static std::string key_of(const char *kind, std::initializer_list<const heal_tensor *> ts, int64_t extra = 0) {
   std::string k(kind);
@@ -786,6 +795,35 @@ int heal_graph_begin(void) {
   HEAL_TRY_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal));
   g_rt.capturing = true;
   g_rt.capture_start = g_rt.launches.load();
+  g_rt.origin = stream();
+  g_rt.forked = 0;
+  return HEAL_OK;
+}
+
+int heal_graph_fork(int n) {
+  clear_error();
+  if (!g_rt.capturing) return set_error(HEAL_ERR_RUNTIME, "heal_graph_fork: not capturing");
+  if (g_rt.forked) return set_error(HEAL_ERR_RUNTIME, "heal_graph_fork: this capture is already forked");
+  if (n < 1 || n > HEAL_GRAPH_MAX_BRANCHES)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_graph_fork: n must be in [1, " + std::to_string(HEAL_GRAPH_MAX_BRANCHES) + "]");
+  if (!g_rt.join) HEAL_TRY_CUDA(cudaEventCreateWithFlags(&g_rt.join, cudaEventDisableTiming));
+  while ((int)g_rt.branches.size() < n) {
+    cudaStream_t s;
+    HEAL_TRY_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    g_rt.branches.push_back(s);
+  }
+  HEAL_TRY_CUDA(cudaEventRecord(g_rt.join, g_rt.origin));
+  for (int i = 0; i < n; ++i) HEAL_TRY_CUDA(cudaStreamWaitEvent(g_rt.branches[i], g_rt.join, 0));
+  g_rt.forked = n;
+  return HEAL_OK;
+}
+
+int heal_graph_branch(int i) {
+  clear_error();
+  if (!g_rt.capturing) return set_error(HEAL_ERR_RUNTIME, "heal_graph_branch: not capturing");
+  if (i < -1 || i >= g_rt.forked)
+    return set_error(HEAL_ERR_OUT_OF_RANGE, "heal_graph_branch: branch " + std::to_string(i) + " was not forked");
+  g_rt.cur = i < 0 ? g_rt.origin : g_rt.branches[i];
   return HEAL_OK;
 }
 
@@ -795,12 +833,24 @@ int heal_graph_end(void **graph) {
   *graph = nullptr;
   if (!g_rt.capturing) return set_error(HEAL_ERR_RUNTIME, "heal_graph_end: not capturing");
   g_rt.capturing = false;
-  cudaGraph_t g = nullptr;
   const uint64_t recorded = g_rt.launches.load() - g_rt.capture_start;
   g_rt.launches.fetch_sub(recorded);  // counted again at every replay
-  HEAL_TRY_CUDA(cudaStreamEndCapture(stream(), &g));
+  // join every branch back into the stream the capture began on
+  cudaError_t je = cudaSuccess;
+  for (int i = 0; i < g_rt.forked && je == cudaSuccess; ++i) {
+    je = cudaEventRecord(g_rt.join, g_rt.branches[i]);
+    if (je == cudaSuccess) je = cudaStreamWaitEvent(g_rt.origin, g_rt.join, 0);
+  }
+  g_rt.forked = 0;
+  g_rt.cur = g_rt.origin;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(g_rt.origin, &g);
+  if (je != cudaSuccess || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(je != cudaSuccess ? je : e, "heal_graph_end");
+  }
   cudaGraphExec_t exec = nullptr;
-  cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+  e = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
   *graph = new HealGraph{exec, recorded};
@@ -823,8 +873,15 @@ int heal_graph_destroy(void *graph) {
   return HEAL_OK;
 }
 
+// calls that wait for the GPU or change the allocation registry cannot be
+// recorded into a graph
+static int refuse_sync(const char *what) {
+  return set_error(HEAL_ERR_RUNTIME, std::string(what) + ": not allowed while a graph is being captured");
+}
+
 int heal_synchronize(void) {
   HEAL_CHECK(ensure_init());
+  if (g_rt.capturing) return refuse_sync("heal_synchronize");
   HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
   flush_diag();
   return HEAL_OK;
@@ -847,6 +904,7 @@ int heal_alloc(size_t bytes, int zero, void **out) {
   if (!out) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_alloc: out must not be null");
   *out = nullptr;
   HEAL_CHECK(ensure_init());
+  if (g_rt.capturing) return refuse_sync("heal_alloc");
   if (bytes == 0) return HEAL_OK;
   void *p = nullptr;
   cudaError_t e = cudaMallocAsync(&p, bytes, stream());
@@ -866,6 +924,7 @@ int heal_alloc(size_t bytes, int zero, void **out) {
 int heal_free(void *ptr) {
   if (!ptr) return HEAL_OK;
   HEAL_CHECK(ensure_init());
+  if (g_rt.capturing) return refuse_sync("heal_free");
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   auto it = g_allocs.find((uintptr_t)ptr);
   if (it == g_allocs.end()) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_free: pointer not from heal_alloc");
@@ -886,6 +945,7 @@ static bool is_pinned(const void *p) {
 
 int heal_h2d(void *dst, const void *src, size_t bytes) {
   HEAL_CHECK(ensure_init());
+  if (g_rt.capturing) return refuse_sync("heal_h2d");
   if (!bytes) return HEAL_OK;
   HEAL_TRY_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream()));
   if (!is_pinned(src)) HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
@@ -895,6 +955,7 @@ int heal_h2d(void *dst, const void *src, size_t bytes) {
 
 int heal_d2h(void *dst, const void *src, size_t bytes) {
   HEAL_CHECK(ensure_init());
+  if (g_rt.capturing) return refuse_sync("heal_d2h");
   if (bytes) HEAL_TRY_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream()));
   HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
   flush_diag();

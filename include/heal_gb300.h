@@ -102,6 +102,18 @@ int heal_graph_end(void **graph);
 int heal_graph_launch(void *graph);
 int heal_graph_destroy(void *graph);
 
+/* Parallel branches inside one capture.  heal_graph_fork(n), once per
+ * capture, starts n branch streams after everything recorded so far;
+ * heal_graph_branch(i) sends the calls that follow to branch i (-1: back to
+ * the stream the capture began on).  heal_graph_end joins every branch, so a
+ * replay ends when all branches have.  Calls on different branches must not
+ * write memory another branch reads or writes.  Synchronising calls
+ * (heal_synchronize, heal_d2h, heal_h2d, heal_alloc, heal_free) fail while a
+ * capture is open. */
+#define HEAL_GRAPH_MAX_BRANCHES 64
+int heal_graph_fork(int n);
+int heal_graph_branch(int i);
+
 /* ------------------------------------------- device memory (HBM residency)
  * Replaces allocate_on_hardware / host_to_device / device_to_host
  * (include/device_memory.h:24-39; example_impl/device_memory_impl.cpp:168-202). */
@@ -211,6 +223,27 @@ int heal_ntt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm
              const heal_tensor *log2p, const heal_tensor *mu, const heal_tensor *result);
 int heal_intt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm, const heal_tensor *inv_twiddles,
               const heal_tensor *m_inv, const heal_tensor *log2p, const heal_tensor *mu, const heal_tensor *result);
+
+/* NTT plans.  A plan fixes, for one element type (HEAL_INT32 / HEAL_INT64),
+ * direction (inverse 0/1), length m and limb count k, the limbs per CTA tile
+ * (1, 2, 4, 8 or 16) and where the butterfly network splits into two passes
+ * (first_pass_log2: log2 of the first pass's length, 1..12 with
+ * log2(m) - first_pass_log2 in 1..12; 0 = one pass, for m <= 4096).  Without
+ * a plan a call uses 4 limbs per tile and one pass up to m = 4096, else an
+ * even split.  Plans change speed only; every plan gives the same result.
+ * No counterpart in HEAL (example_impl has one loop nest). */
+int heal_ntt_set_plan(int dtype, int inverse, int64_t m, int64_t k, int tile_limbs, int first_pass_log2);
+/* The plan a call of this shape uses: the one set, else the default. */
+int heal_ntt_get_plan(int dtype, int inverse, int64_t m, int64_t k, int *tile_limbs, int *first_pass_log2);
+int heal_ntt_clear_plans(void);
+/* Times every candidate plan on these operands (heal_ntt when inverse == 0,
+ * else heal_intt with m_inv) with `reps` calls each and keeps the fastest for
+ * this shape; `result` is overwritten.  The choice is returned through
+ * tile_limbs / first_pass_log2 (either may be null).  Waits for the GPU; fails
+ * while a graph is being captured. */
+int heal_ntt_autotune(int inverse, const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm,
+                      const heal_tensor *twiddles, const heal_tensor *m_inv, const heal_tensor *result, int reps,
+                      int *tile_limbs, int *first_pass_log2);
 
 /* Per-row gather along perm_axis with indices perms[l, m]
  * (include/permute.h:33-40; example_impl/permute_impl.cpp:8-65). */

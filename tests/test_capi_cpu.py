@@ -96,3 +96,30 @@ def test_contiguity_and_span():
     assert L.heal_tensor_span(ctypes.byref(t((4, 3), (1, 4)))) == 12
     assert L.heal_tensor_span(ctypes.byref(t((3, 4), (0, 1)))) == 4
     assert L.heal_tensor_span(ctypes.byref(t((0, 4)))) == 0
+
+
+def test_ntt_plan_table_host_side():
+    L = capi.lib()
+    I64, I32 = capi.DTYPES[np.dtype(np.int64)], capi.DTYPES[np.dtype(np.int32)]
+    try:
+        assert capi.ntt_plan(np.int64, False, 1 << 16, 24) == (4, 8)     # default: even split
+        assert capi.ntt_plan(np.int32, True, 1 << 12, 4) == (4, 0)       # one pass
+        capi.check(L.heal_ntt_set_plan(I64, 0, 1 << 16, 24, 8, 6))
+        assert capi.ntt_plan(np.int64, False, 1 << 16, 24) == (8, 6)
+        assert capi.ntt_plan(np.int64, True, 1 << 16, 24) == (4, 8)       # per direction
+        assert capi.ntt_plan(np.int64, False, 1 << 16, 23) == (4, 8)      # per limb count
+        bad = [(I64, 0, 1 << 16, 24, 3, 8),      # tile width not a power of two
+               (I64, 0, 1 << 16, 24, 32, 8),     # too wide
+               (I64, 0, 1 << 16, 24, 4, 0),      # one pass above 4096 points
+               (I64, 0, 1 << 16, 24, 4, 3),      # second pass of 13 stages
+               (I64, 0, 1 << 16, 24, 4, 16),     # empty second pass
+               (I32, 0, 3000, 4, 4, 0),          # not a power of two
+               (2, 0, 1 << 10, 4, 4, 0),         # float64
+               (I64, 2, 1 << 10, 4, 4, 0),       # direction
+               (I64, 0, 1 << 10, 0, 4, 0)]       # no limbs
+        for args in bad:
+            assert L.heal_ntt_set_plan(*args) == 1, args
+            assert L.heal_last_error()
+    finally:
+        capi.check(L.heal_ntt_clear_plans())
+    assert capi.ntt_plan(np.int64, False, 1 << 16, 24) == (4, 8)
