@@ -326,11 +326,25 @@ def our_arm(args):
 
 
 def other_configs(args, timed, stream):
-    """cfg1 (plain and as one CUDA graph) and cfg4, timed like the headline."""
+    """The other configurations, timed like the headline: cfg1 (plain and as
+    one CUDA graph), cfg4, cfg3 (ragged batch) and cfg5 (serving loop)."""
+    out = {}
+    want = set(args.configs.split(","))
+    if "cfg1" in want:
+        out["cfg1"] = cfg1_config(args, timed)
+    if "cfg4" in want:
+        out["cfg4"] = cfg4_config(args, timed)
+    if "cfg3" in want:
+        out["cfg3"] = ragged_config(args, timed)
+    if "cfg5" in want:
+        out["cfg5"] = serving_config(args)
+    return out
+
+
+def cfg1_config(args, timed):
     import hashlib
     from heal_gb300 import capi
-    from heal_gb300.configs import Cfg1, Cfg4
-    out = {}
+    from heal_gb300.configs import Cfg1
     c1 = Cfg1()
     c1.run()
     with open(os.path.join(ROOT, "tests", "golden", "golden_hash.json")) as f:
@@ -346,12 +360,15 @@ def other_configs(args, timed, stream):
         graph.launch()
     ms_graph, l_graph = timed(lambda s: graph.launch(), steps)
     exact = exact and sha(c1.AS) == gh["axis_modsum"]
-    out["cfg1"] = {"workload": "ntt(A), ntt(B), intt(ntt(A)), modmul, axis_modsum over the batch; [8, 4096, 1, 4] "
-                               "int64, 30-bit primes", "bit_exact_vs_reference_hashes": exact,
-                   "step_us_plain": ms_plain / steps * 1e3, "step_us_graph": ms_graph / steps * 1e3,
-                   "transform_limbs_per_s_graph": c1.transform_limbs() * steps / (ms_graph / 1e3),
-                   "launches_per_step": l_graph / steps}
-    del graph
+    return {"workload": "ntt(A), ntt(B), intt(ntt(A)), modmul, axis_modsum over the batch; [8, 4096, 1, 4] "
+                        "int64, 30-bit primes", "bit_exact_vs_reference_hashes": exact,
+            "step_us_plain": ms_plain / steps * 1e3, "step_us_graph": ms_graph / steps * 1e3,
+            "transform_limbs_per_s_graph": c1.transform_limbs() * steps / (ms_graph / 1e3),
+            "launches_per_step": l_graph / steps}
+
+
+def cfg4_config(args, timed):
+    from heal_gb300.configs import Cfg4
     c4 = Cfg4()
     c4.ntt()
     c4.intt()
@@ -361,12 +378,9 @@ def other_configs(args, timed, stream):
     ms4i, _ = timed(lambda s: c4.intt(), st4)
     hbm, _ = peaks()
     per = ms4 / st4
-    out["cfg4"] = {"workload": "ntt on [64, 65536, 1, 32] int32, 31-bit primes, radix-8 Shoup butterflies on the integer pipes",
-                   "ntt_ms": per, "intt_ms": ms4i / st4, "limbs_per_s": c4.limbs() / (per / 1e3),
-                   "hbm_frac": c4.bytes_per_call() / (per / 1e3) / 1e9 / hbm, "round_trip_exact": round_trip}
-    del c4
-    out["cfg3"] = ragged_config(args, timed)
-    return out
+    return {"workload": "ntt on [64, 65536, 1, 32] int32, 31-bit primes, radix-8 Shoup butterflies on the integer "
+                        "pipes", "ntt_ms": per, "intt_ms": ms4i / st4, "limbs_per_s": c4.limbs() / (per / 1e3),
+            "hbm_frac": c4.bytes_per_call() / (per / 1e3) / 1e9 / hbm, "round_trip_exact": round_trip}
 
 
 def ragged_config(args, timed):
@@ -419,6 +433,55 @@ def ragged_config(args, timed):
             "autotuned_shapes": len(shapes), "autotune_s": tune_s, "setup_s": setup_s,
             "plans_sample": {f"{n}x{l}": {"fwd": plans[(n, l)][0], "inv": plans[(n, l)][1]}
                              for n, l in shapes[:: max(1, len(shapes) // 6)]}}
+
+
+def serving_config(args, count: int = 4000, rate: float = 2000.0):
+    """cfg5: Poisson arrivals of ciphertext x plaintext-matrix products
+    admitted by HBM footprint; served with the three HEAL calls (permute
+    rotations, modmul, axis_modsum) and with the fused modmul_axis_sum."""
+    out = {"workload": f"{count} Poisson arrivals at {rate:.0f}/s of ct[2][N][L] x (d x d plaintext matrix): "
+                       "d in {16, 64, 256}, N in {2^14, 2^15}, L uniform in 8..16, 40-bit primes; sum over d Galois "
+                       "rotations of rot_i(ct) * diag_i, H2D of the matrix and D2H of the result per request"}
+    for name, fused in (("three_calls", False), ("fused", True)):
+        out[name] = serve_once(count, rate, fused)
+    return out
+
+
+def serve_once(count, rate, fused):
+    import torch
+    from heal_gb300 import serving as S
+    t0 = time.time()
+    srv = S.MatVecServer(fused=fused)
+    srv.warm()
+    setup_s = time.time() - t0
+    alone_ms = {}
+    for d in srv.ds:                                   # service time of the largest request of each d
+        r = S.Request(-1, 0.0, max(srv.ns), srv.lmax, d, 0, 0)
+        ts = []
+        for _ in range(5):
+            t1 = time.perf_counter()
+            srv.alone(r)
+            ts.append((time.perf_counter() - t1) * 1e3)
+        alone_ms[str(d)] = statistics.median(ts)
+    big = S.Request(-1, 0.0, max(srv.ns), srv.lmax, max(srv.ds), 0, 0)
+    split = srv.split_ms(big)
+    reqs = S.poisson_schedule(count, rate, 606, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
+    sample = [r.rid for r in reqs[:: count // 8]]
+    st = srv.run(reqs, keep=sample)
+    torch.cuda.synchronize()
+    same = all(np.array_equal(srv.out_host[i], srv.alone(reqs[i])) for i in sample)
+    moved = sum(S.MatVecServer.bytes_moved(r) for r in reqs)
+    ms = lambda xs, q: S.percentile(xs, q) * 1e3
+    res = {"p50_ms": ms(st.latencies, 50), "p99_ms": ms(st.latencies, 99),
+           "mean_ms": float(np.mean(st.latencies)) * 1e3,
+           "p50_wait_ms": ms(st.waits, 50), "p99_wait_ms": ms(st.waits, 99),
+           "throughput_req_per_s": count / st.span, "offered_req_per_s": count / reqs[-1].arrival,
+           "algorithmic_GBps": moved / st.span / 1e9, "max_inflight": st.max_inflight, "max_queue": st.max_queue,
+           "arena_GiB": srv.arena_size / 2**30, "peak_arena_GiB": st.peak_bytes / 2**30, "streams": len(srv.streams),
+           "service_ms_alone_largest": alone_ms, "alone_equals_mix": same, "setup_s": setup_s,
+           "split_ms_largest": split, "largest_request_bytes": S.MatVecServer.bytes_moved(big)}
+    del srv
+    return res
 
 
 def ntt_probe(args):
@@ -474,6 +537,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-configs", action="store_true")
+    ap.add_argument("--configs", default="cfg1,cfg3,cfg4,cfg5",
+                    help="comma-separated configurations reported beside the headline")
     ap.add_argument("--mode", default="chain", choices=["chain", "ntt"])
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--probe", default="digits", choices=["digits", "cfg4"])

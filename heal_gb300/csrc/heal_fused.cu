@@ -1,0 +1,297 @@
+// heal_fused.cu — modmul_axis_sum, the fused compute op that HEAL's Python
+// runtime routes to its backend (python_execution/lattica_heal_runtime/
+// device_interface.py:67-68; HEAL names the op and leaves its definition to
+// the backend).  Defined here as the composition of HEAL's own ops
+//
+//   result = axis_modsum(modmul(a', b, p), axis)
+//
+// with a and b broadcast like modmul (example_impl/modop_impl.cpp:44-101) to
+// a common shape S, and a' = a or, with `perms`, a gathered like permute
+// with elementwise_axis = axis (example_impl/permute_impl.cpp:8-65):
+// a'[c] = a[c with c[perm_axis] <- perms[c[axis], c[perm_axis]]].
+// The product is never written: one thread per result element runs the
+// reduction, so a rotate-multiply-accumulate over d rotations reads the
+// rotated operand (resident in L2) and b once and writes only the result.
+//
+// Arithmetic.  With every term canonical (0 <= a', b < q) the running sum of
+// residues equals (sum of products) mod q, so the products are accumulated
+// exactly in 128 bits (64-bit words; high word kept below q by subtracting
+// q * 2^64) or 64 bits (32-bit words; kept below q * 2^32) and reduced once
+// (Moller-Granlund).  An element with any other term is recomputed term by
+// term with the reference's semantics: modmul's C '%' in the double-width
+// type, then axis_modsum's running (sum + v) % q.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "heal_internal.h"
+
+namespace heal {
+
+struct FusedArgs {
+  View r;                 // result view
+  View ao, bo;            // a and b strides in result coordinates
+  int64_t a_ax, b_ax;     // strides along the reduced axis
+  int64_t len;            // reduced length
+  int pa;                 // perm axis in result coordinates, -1 without perms
+  int last;               // last axis in result coordinates
+  int64_t a_pa;           // a's stride along the perm axis
+  int64_t ps0, ps1;       // perms strides
+  const void *a, *b, *perms;
+  int perms_dtype;
+  const void *ptab;       // MG64 / MG32 per modulus
+  void *out;
+  int64_t n;
+  FastDims fd;
+  Diag *diag;
+};
+
+template <typename T> struct FusedMG;
+template <> struct FusedMG<int32_t> { typedef MG32 type; };
+template <> struct FusedMG<int64_t> { typedef MG64 type; };
+
+__device__ __forceinline__ int64_t fused_perm(const FusedArgs &g, int64_t i, int64_t c) {
+  return g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[i * g.ps0 + c * g.ps1]
+                                     : ((const int64_t *)g.perms)[i * g.ps0 + c * g.ps1];
+}
+
+// one term's element of modmul then one step of axis_modsum's running sum,
+// as the separate kernels compute them
+template <typename T>
+__device__ __forceinline__ int64_t exact_step(int64_t sum, int64_t a, int64_t b, int64_t q,
+                                              const typename FusedMG<T>::type &c) {
+  int64_t v;
+  if (a >= 0 && b >= 0 && q > 0) {
+    if (sizeof(T) == 4) v = (int64_t)(T)mg32_mod((uint64_t)a * (uint64_t)b, (const MG32 &)c);
+    else v = (int64_t)(T)mg64_mulmod((uint64_t)a, (uint64_t)b, (const MG64 &)c);
+  } else {
+    v = (int64_t)(T)((i128)a * (i128)b % (i128)q);
+  }
+  if (sum >= 0 && v >= 0 && q > 0) {
+    uint64_t x = (uint64_t)sum + (uint64_t)v;
+    return v < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
+  }
+  return crem128((i128)sum + (i128)v, q);
+}
+
+constexpr int kFusedU = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_constant__ FusedArgs g) {
+  typedef typename FusedMG<T>::type M;
+  const T *A = (const T *)g.a;
+  const T *B = (const T *)g.b;
+  T *R = (T *)g.out;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t a0 = 0, b0 = 0, r0 = 0, t = 0, cp = 0;
+    if (g.fd.fast) {
+      uint32_t rem = (uint32_t)idx;
+      for (int i = g.r.ndim - 1; i >= 0; --i) {
+        const uint32_t qd = fastdiv(rem, g.fd.fd[i]);
+        const int64_t c = rem - qd * (uint32_t)g.r.dims[i];
+        rem = qd;
+        if (i == g.last) t = c;
+        if (i == g.pa) cp = c;
+        a0 += c * g.ao.strides[i];
+        b0 += c * g.bo.strides[i];
+        r0 += c * g.r.strides[i];
+      }
+    } else {
+      int64_t rem = idx;
+      for (int i = g.r.ndim - 1; i >= 0; --i) {
+        const int64_t c = rem % g.r.dims[i];
+        rem /= g.r.dims[i];
+        if (i == g.last) t = c;
+        if (i == g.pa) cp = c;
+        a0 += c * g.ao.strides[i];
+        b0 += c * g.bo.strides[i];
+        r0 += c * g.r.strides[i];
+      }
+    }
+    const M mc = ((const M *)g.ptab)[t];
+    const int64_t q = sizeof(T) == 4 ? (int64_t)(int32_t)((const MG32 &)mc).q : (int64_t)((const MG64 &)mc).q;
+    if (q == 0) {  // modmul and axis_modsum both give 0 for a zero modulus
+      atomicAdd(&g.diag->zero_mod, 1ull);
+      R[r0] = 0;
+      continue;
+    }
+    const bool perm = g.pa >= 0;
+    bool canon = q > 0;
+    uint64_t hi = 0, lo = 0;  // 64-bit words: hi * 2^64 + lo, hi < q; 32-bit words: lo < q * 2^32
+    const uint64_t uq = (uint64_t)q, q32 = uq << 32;
+    for (int64_t i0 = 0; i0 < g.len && canon; i0 += kFusedU) {
+      int64_t aoff[kFusedU];
+#pragma unroll
+      for (int u = 0; u < kFusedU; ++u) {
+        const int64_t i = i0 + u < g.len ? i0 + u : i0;
+        aoff[u] = a0 + i * g.a_ax + (perm ? fused_perm(g, i, cp) * g.a_pa : 0);
+      }
+      int64_t av[kFusedU], bv[kFusedU];
+#pragma unroll
+      for (int u = 0; u < kFusedU; ++u) {
+        const int64_t i = i0 + u < g.len ? i0 + u : i0;
+        av[u] = (int64_t)A[aoff[u]];
+        bv[u] = (int64_t)B[b0 + i * g.b_ax];
+      }
+#pragma unroll
+      for (int u = 0; u < kFusedU; ++u) {
+        if (i0 + u >= g.len) break;
+        const uint64_t x = (uint64_t)av[u], y = (uint64_t)bv[u];
+        canon = canon && x < uq && y < uq;  // also rejects negative values
+        if (sizeof(T) == 4) {
+          lo += x * y;                      // < 2 q 2^32 < 2^64
+          lo = lo >= q32 ? lo - q32 : lo;
+        } else {
+          const uint64_t plo = x * y, phi = mulhi64(x, y);
+          const uint64_t s = lo + plo;
+          hi += phi + (s < lo ? 1 : 0);     // < 2q
+          lo = s;
+          hi = hi >= uq ? hi - uq : hi;
+        }
+      }
+    }
+    int64_t res;
+    if (canon) {
+      res = sizeof(T) == 4 ? (int64_t)mg32_mod(lo, (const MG32 &)mc) : (int64_t)mg64_mod(hi, lo, (const MG64 &)mc);
+    } else {
+      res = 0;
+      for (int64_t i = 0; i < g.len; ++i) {
+        const int64_t aoffs = a0 + i * g.a_ax + (perm ? fused_perm(g, i, cp) * g.a_pa : 0);
+        res = exact_step<T>(res, (int64_t)A[aoffs], (int64_t)B[b0 + i * g.b_ax], q, mc);
+      }
+    }
+    R[r0] = (T)res;
+  }
+}
+
+static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
+                 int64_t perm_axis, const heal_tensor *r, int64_t axis) {
+  clear_error();
+  HEAL_CHECK(check_desc(a, "a", true));
+  HEAL_CHECK(check_desc(b, "b", true));
+  HEAL_CHECK(check_desc(p, "p", true));
+  if (perms) HEAL_CHECK(check_desc(perms, "perms", true));
+  HEAL_CHECK(check_desc(r, "result", true));
+  HEAL_CHECK(ensure_init());
+  const int dt = r->dtype;
+  if (a->dtype != dt || b->dtype != dt || p->dtype != dt)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "all tensors must have the element type of result");
+  // common shape of a and b, right-aligned as modmul broadcasts
+  const int nd = std::max(a->ndim, b->ndim);
+  if (nd < 2) return set_error(HEAL_ERR_INVALID_ARGUMENT, "a and b must have at least 2 dimensions");
+  int64_t S[HEAL_MAX_DIMS];
+  for (int i = 0; i < nd; ++i) {
+    const int ia = i - (nd - a->ndim), ib = i - (nd - b->ndim);
+    const int64_t da = ia >= 0 ? a->dims[ia] : 1, db = ib >= 0 ? b->dims[ib] : 1;
+    if (da != db && da != 1 && db != 1)
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "a and b are not broadcast-compatible.");
+    S[i] = da == 1 ? db : da;
+  }
+  if (axis < 0 || axis >= nd - 1)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "axis must be in range [0, ndim - 2] (can't reduce across last axis)");
+  if (p->ndim != 1 || p->dims[0] != S[nd - 1])
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "p must be a 1D tensor of shape [k], k the last dimension");
+  if (r->ndim != nd - 1)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "Result must have the shape of a and b with the reduced axis removed.");
+  for (int i = 0, j = 0; i < nd; ++i) {
+    if (i == axis) continue;
+    if (r->dims[j++] != S[i])
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "Result must have the shape of a and b with the reduced axis removed.");
+  }
+  if (perms) {
+    if (perm_axis < 0 || perm_axis >= nd) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Axis out of bounds.");
+    if (perm_axis == axis) return set_error(HEAL_ERR_INVALID_ARGUMENT, "axis and perm_axis must be different.");
+    if (perms->ndim != 2 || perms->dims[0] != S[axis] || perms->dims[1] != S[perm_axis])
+      return set_error(HEAL_ERR_INVALID_ARGUMENT,
+                       "Perms must have shape [l, m] where l and m match the shape at axis and perm_axis.");
+  }
+  const int64_t n = numel(*r);
+  if (n == 0) return HEAL_OK;
+  if (perms && S[axis] > 0) {
+    bool valid = false;
+    HEAL_CHECK(perms_valid(*perms, S[perm_axis], &valid));
+    if (!valid) return set_error(HEAL_ERR_OUT_OF_RANGE, "Permutation index out of bounds.");
+  }
+  heal_tensor A = *a, B = *b, P = *p, PR = perms ? *perms : heal_tensor();
+  void *owned[4] = {nullptr, nullptr, nullptr, nullptr};
+  auto detach = [&](heal_tensor &t, int slot) -> int {
+    return overlaps(t, *r) ? materialize(t, &t, &owned[slot]) : HEAL_OK;
+  };
+  int rc = detach(A, 0);
+  if (!rc) rc = detach(B, 1);
+  if (!rc) rc = detach(P, 2);
+  if (!rc && perms) rc = detach(PR, 3);
+  ModTable mt;
+  if (!rc) rc = mod_table(P, &mt);
+  if (!rc) {
+    FusedArgs g;
+    memset(&g, 0, sizeof g);
+    // strides of a and b in S coordinates (0 on broadcast axes)
+    int64_t as[HEAL_MAX_DIMS], bs[HEAL_MAX_DIMS];
+    for (int i = 0; i < nd; ++i) {
+      const int ia = i - (nd - A.ndim), ib = i - (nd - B.ndim);
+      as[i] = (ia >= 0 && A.dims[ia] != 1) ? A.strides[ia] : 0;
+      bs[i] = (ib >= 0 && B.dims[ib] != 1) ? B.strides[ib] : 0;
+    }
+    g.r = make_view(*r);
+    g.ao = g.r;
+    g.bo = g.r;
+    for (int i = 0, j = 0; i < nd; ++i) {
+      if (i == axis) continue;
+      g.ao.strides[j] = (perms && i == perm_axis) ? 0 : as[i];
+      g.bo.strides[j] = bs[i];
+      ++j;
+    }
+    g.a_ax = as[axis];
+    g.b_ax = bs[axis];
+    g.len = S[axis];
+    g.a_pa = perms ? as[perm_axis] : 0;
+    int pa = perms ? (int)(perm_axis < axis ? perm_axis : perm_axis - 1) : -1;
+    int last = nd - 2;
+    // merge axes other than the two whose coordinates the kernel reads
+    unsigned keep = 1u << last;
+    if (pa >= 0) keep |= 1u << pa;
+    View *vs[3] = {&g.r, &g.ao, &g.bo};
+    int map[HEAL_MAX_DIMS];
+    coalesce_views(vs, 3, keep, map);
+    g.pa = pa >= 0 ? map[pa] : -1;
+    g.last = map[last];
+    make_fast_dims(g.r, n, &g.fd);
+    g.ps0 = perms ? PR.strides[0] : 0;
+    g.ps1 = perms ? PR.strides[1] : 0;
+    g.a = A.data;
+    g.b = B.data;
+    g.perms = perms ? PR.data : nullptr;
+    g.perms_dtype = perms ? PR.dtype : HEAL_INT64;
+    g.ptab = mt.consts;
+    g.out = r->data;
+    g.n = n;
+    g.diag = diag_device();
+    const int threads = 256;
+    const int64_t want = (n + threads - 1) / threads;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * 16));
+    if (dt == HEAL_INT32)
+      modmul_axis_sum_kernel<int32_t><<<grid, threads, 0, stream()>>>(g);
+    else
+      modmul_axis_sum_kernel<int64_t><<<grid, threads, 0, stream()>>>(g);
+    rc = check_launch("modmul_axis_sum");
+  }
+  for (void *o : owned) scratch_free(o);
+  if (!rc) mark_written(r->data);
+  return rc;
+}
+
+}  // namespace heal
+
+using namespace heal;
+
+extern "C" {
+
+int heal_modmul_axis_sum(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
+                         int64_t perm_axis, const heal_tensor *result, int64_t axis) {
+  return fused(a, b, p, perms, perm_axis, result, axis);
+}
+
+}  // extern "C"

@@ -119,21 +119,4 @@ int perms_valid(const heal_tensor &perms, int64_t m, bool *ok);
 
 }  // namespace heal
 
-// ------------------------------------------------- device-side tensor view
-namespace heal {
-struct View {
-  int64_t dims[HEAL_MAX_DIMS];
-  int64_t strides[HEAL_MAX_DIMS];
-  int32_t ndim;
-};
-
-inline View make_view(const heal_tensor &t) {
-  View v;
-  v.ndim = t.ndim;
-  for (int i = 0; i < HEAL_MAX_DIMS; ++i) {
-    v.dims[i] = i < t.ndim ? t.dims[i] : 1;
-    v.strides[i] = i < t.ndim ? t.strides[i] : 0;
-  }
-  return v;
-}
-}  // namespace heal
+#include "heal_view.h"

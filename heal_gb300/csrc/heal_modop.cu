@@ -40,6 +40,7 @@ struct ModopArgs {
   int64_t last;        // result's last dimension (dense kernel)
   FastDiv last_div;    // division by `last` (dense kernel, n < 2^32)
   int p_per_last;      // dense kernel: modulus index = coordinate on the last axis
+  FastDims fd;         // general kernel: 32-bit decomposition of r's coordinates
   Diag *diag;
 };
 
@@ -204,29 +205,63 @@ __global__ void __launch_bounds__(256) modop_dense_kernel(const __grid_constant_
 }
 
 // ---------------------------------------------------- general kernel
+// Any strides (broadcast axes have stride 0), axes merged on the host where
+// every operand allows.  Each thread takes kGenU elements a block-width
+// apart per iteration and issues all their loads before the arithmetic, so
+// enough bytes are in flight to cover HBM latency.
+constexpr int kGenU = 4;
+
 template <typename T, int OP>
 __global__ void __launch_bounds__(256) modop_general_kernel(const __grid_constant__ ModopArgs g) {
+  typedef typename MGOf<T>::type M;
   const T *A = (const T *)g.ap;
   const T *B = (const T *)g.bp;
-  const T *P = (const T *)g.pp;
   T *R = (T *)g.rp;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t rem = idx, oa = 0, ob = 0, op = 0, orr = 0, opd = 0;
-    for (int i = g.r.ndim - 1; i >= 0; --i) {
-      int64_t d = g.r.dims[i];
-      int64_t c = rem % d;
-      rem /= d;
-      oa += c * g.a.strides[i];
-      ob += c * g.b.strides[i];
-      op += c * g.p.strides[i];
-      opd += c * g.pd.strides[i];
-      orr += c * g.r.strides[i];
+  const int64_t step = (int64_t)gridDim.x * blockDim.x * kGenU;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * kGenU + threadIdx.x; base < g.n; base += step) {
+    int64_t oa[kGenU], ob[kGenU], orr[kGenU], opd[kGenU];
+#pragma unroll
+    for (int u = 0; u < kGenU; ++u) {
+      const int64_t idx = base + (int64_t)u * blockDim.x;
+      oa[u] = ob[u] = orr[u] = opd[u] = 0;
+      if (idx >= g.n) continue;
+      if (g.fd.fast) {
+        uint32_t rem = (uint32_t)idx;
+        for (int i = g.r.ndim - 1; i >= 0; --i) {
+          const uint32_t q = fastdiv(rem, g.fd.fd[i]);
+          const int64_t c = rem - q * (uint32_t)g.r.dims[i];
+          rem = q;
+          oa[u] += c * g.a.strides[i];
+          ob[u] += c * g.b.strides[i];
+          opd[u] += c * g.pd.strides[i];
+          orr[u] += c * g.r.strides[i];
+        }
+      } else {
+        int64_t rem = idx;
+        for (int i = g.r.ndim - 1; i >= 0; --i) {
+          const int64_t d = g.r.dims[i];
+          const int64_t c = rem % d;
+          rem /= d;
+          oa[u] += c * g.a.strides[i];
+          ob[u] += c * g.b.strides[i];
+          opd[u] += c * g.pd.strides[i];
+          orr[u] += c * g.r.strides[i];
+        }
+      }
     }
-    typename MGOf<T>::type c = mg_of<T>(g, opd);
-    int64_t p = P ? (int64_t)P[op] : g.ps;
-    int64_t b = B ? (int64_t)B[ob] : g.bs;
-    R[orr] = elem_op<T, OP>((int64_t)A[oa], b, p, c, g.diag);
+    int64_t av[kGenU], bv[kGenU];
+    M cv[kGenU];
+#pragma unroll
+    for (int u = 0; u < kGenU; ++u) {
+      const bool in = base + (int64_t)u * blockDim.x < g.n;
+      av[u] = in ? (int64_t)A[oa[u]] : 0;
+      bv[u] = (in && B) ? (int64_t)B[ob[u]] : g.bs;
+      cv[u] = mg_of<T>(g, in ? opd[u] : 0);
+    }
+#pragma unroll
+    for (int u = 0; u < kGenU; ++u)
+      if (base + (int64_t)u * blockDim.x < g.n)
+        R[orr[u]] = elem_op<T, OP>(av[u], bv[u], q_of<T>(g, cv[u]), cv[u], g.diag);
   }
 }
 
@@ -346,7 +381,7 @@ static int launch(ModopArgs &g, bool dense) {
     else
       launch_dense<T, OP, 1>(g, s, want);
   } else {
-    modop_general_kernel<T, OP><<<grid_for(g.n, 256, 8), 256, 0, s>>>(g);
+    modop_general_kernel<T, OP><<<grid_for((g.n + kGenU - 1) / kGenU, 256, 8), 256, 0, s>>>(g);
   }
   return check_launch("modop");
 }
@@ -431,6 +466,12 @@ static int modop(int op, const heal_tensor *a, const heal_tensor *b, int64_t bs,
     }
     if (dense && g.last > 0 && g.last < (int64_t)UINT32_MAX) g.last_div = fastdiv_make((uint32_t)g.last);
     else dense = dense && !g.p_per_last;
+    if (!dense) {
+      // general kernel: merge axes that every operand walks linearly
+      View *vs[4] = {&g.r, &g.a, &g.b, &g.pd};
+      coalesce_views(vs, 4, 0u, nullptr);
+      make_fast_dims(g.r, n, &g.fd);
+    }
     if (op == OP_MOD) {
       // mod_tt / tc / ct: a and b play the roles of dividend and divisor
       rc = dt == HEAL_INT32 ? launch<int32_t, OP_MOD>(g, dense) : launch<int64_t, OP_MOD>(g, dense);

@@ -90,14 +90,22 @@ __global__ void __launch_bounds__(256) axis_modsum_kernel(const __grid_constant_
       R[orr] = 0;
       continue;
     }
+    // the reference's running sum, in order; loads go out kBatch at a time
+    constexpr int kBatch = 8;
     int64_t sum = 0;
-    for (int64_t k = 0; k < g.ax_len; ++k) {
-      int64_t v = (int64_t)A[oa + k * g.ax_stride];
-      if (sum >= 0 && v >= 0 && q > 0) {
-        uint64_t x = (uint64_t)sum + (uint64_t)v;
-        sum = v < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
-      } else {
-        sum = crem128((i128)sum + (i128)v, q);
+    for (int64_t k0 = 0; k0 < g.ax_len; k0 += kBatch) {
+      int64_t v[kBatch];
+#pragma unroll
+      for (int j = 0; j < kBatch; ++j) v[j] = k0 + j < g.ax_len ? (int64_t)A[oa + (k0 + j) * g.ax_stride] : 0;
+#pragma unroll
+      for (int j = 0; j < kBatch; ++j) {
+        if (k0 + j >= g.ax_len) break;
+        if (sum >= 0 && v[j] >= 0 && q > 0) {
+          uint64_t x = (uint64_t)sum + (uint64_t)v[j];
+          sum = v[j] < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
+        } else {
+          sum = crem128((i128)sum + (i128)v[j], q);
+        }
       }
     }
     R[orr] = (T)sum;
@@ -367,56 +375,92 @@ struct PermuteArgs {
   int ew_in_post;
   int fast;                 // n below 2^32: 32-bit divisions below
   FastDiv f_post, f_m, f_ewdiv, f_ewmod;
+  FastDims fd;              // general path: 32-bit decomposition of r's coordinates
 };
 
+__device__ __forceinline__ int64_t perm_at(const PermuteArgs &g, int64_t e, int64_t pm) {
+  return g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[e * g.ps0 + pm * g.ps1]
+                                     : ((const int64_t *)g.perms)[e * g.ps0 + pm * g.ps1];
+}
+
+// row-major a and result: idx = (pre * m + pm) * post + inner
 template <typename T>
-__global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ PermuteArgs g) {
+__global__ void __launch_bounds__(256) permute_dense_kernel(const __grid_constant__ PermuteArgs g) {
   const T *A = (const T *)g.src;
   T *R = (T *)g.out;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t src, dst;
-    if (g.dense) {
-      int64_t inner, pm, pre, e;
-      if (g.fast) {
-        const uint32_t x = (uint32_t)idx;
-        const uint32_t rest = fastdiv(x, g.f_post);
-        inner = x - rest * (uint32_t)g.post;
-        const uint32_t pr = fastdiv(rest, g.f_m);
-        pm = rest - pr * (uint32_t)g.m;
-        pre = pr;
-        const uint32_t y = fastdiv((uint32_t)(g.ew_in_post ? inner : pre), g.f_ewdiv);
-        e = y - fastdiv(y, g.f_ewmod) * (uint32_t)g.ew_mod;
-      } else {
-        inner = idx % g.post;
-        const int64_t rest = idx / g.post;
-        pm = rest % g.m;
-        pre = rest / g.m;
-        e = ((g.ew_in_post ? inner : pre) / g.ew_div) % g.ew_mod;
-      }
-      int64_t pidx = g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[e * g.ps0 + pm * g.ps1]
-                                                 : ((const int64_t *)g.perms)[e * g.ps0 + pm * g.ps1];
-      src = (pre * g.m + pidx) * g.post + inner;
-      dst = idx;
+    int64_t inner, pm, pre, e;
+    if (g.fast) {
+      const uint32_t x = (uint32_t)idx;
+      const uint32_t rest = fastdiv(x, g.f_post);
+      inner = x - rest * (uint32_t)g.post;
+      const uint32_t pr = fastdiv(rest, g.f_m);
+      pm = rest - pr * (uint32_t)g.m;
+      pre = pr;
+      const uint32_t y = fastdiv((uint32_t)(g.ew_in_post ? inner : pre), g.f_ewdiv);
+      e = y - fastdiv(y, g.f_ewmod) * (uint32_t)g.ew_mod;
     } else {
-      int64_t c[HEAL_MAX_DIMS];
-      int64_t rem = idx;
-      for (int i = g.r.ndim - 1; i >= 0; --i) {
-        c[i] = rem % g.r.dims[i];
-        rem /= g.r.dims[i];
-      }
-      int64_t e = c[g.ew], pm = c[g.pa];
-      int64_t pidx = g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[e * g.ps0 + pm * g.ps1]
-                                                 : ((const int64_t *)g.perms)[e * g.ps0 + pm * g.ps1];
-      c[g.pa] = pidx;
-      src = 0;
-      dst = 0;
-      for (int i = 0; i < g.r.ndim; ++i) {
-        src += c[i] * g.a.strides[i];
-        dst += (i == g.pa ? pm : c[i]) * g.r.strides[i];
-      }
+      inner = idx % g.post;
+      const int64_t rest = idx / g.post;
+      pm = rest % g.m;
+      pre = rest / g.m;
+      e = ((g.ew_in_post ? inner : pre) / g.ew_div) % g.ew_mod;
     }
-    R[dst] = A[src];
+    R[idx] = A[(pre * g.m + perm_at(g, e, pm)) * g.post + inner];
+  }
+}
+
+// any strides (axes merged on the host except the two it reads); kGenU
+// elements per thread per iteration, loads issued together
+constexpr int kGenU = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(256) permute_general_kernel(const __grid_constant__ PermuteArgs g) {
+  const T *A = (const T *)g.src;
+  T *R = (T *)g.out;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x * kGenU;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * kGenU + threadIdx.x; base < g.n; base += step) {
+    int64_t src[kGenU], dst[kGenU];
+#pragma unroll
+    for (int u = 0; u < kGenU; ++u) {
+      const int64_t idx = base + (int64_t)u * blockDim.x;
+      int64_t e = 0, pm = 0, s = 0, d = 0;
+      if (idx < g.n) {
+        if (g.fd.fast) {
+          uint32_t rem = (uint32_t)idx;
+          for (int i = g.r.ndim - 1; i >= 0; --i) {
+            const uint32_t q = fastdiv(rem, g.fd.fd[i]);
+            const int64_t c = rem - q * (uint32_t)g.r.dims[i];
+            rem = q;
+            if (i == g.ew) e = c;
+            if (i == g.pa) pm = c;
+            else s += c * g.a.strides[i];
+            d += c * g.r.strides[i];
+          }
+        } else {
+          int64_t rem = idx;
+          for (int i = g.r.ndim - 1; i >= 0; --i) {
+            const int64_t c = rem % g.r.dims[i];
+            rem /= g.r.dims[i];
+            if (i == g.ew) e = c;
+            if (i == g.pa) pm = c;
+            else s += c * g.a.strides[i];
+            d += c * g.r.strides[i];
+          }
+        }
+        s += perm_at(g, e, pm) * g.a.strides[g.pa];
+      }
+      src[u] = s;
+      dst[u] = d;
+    }
+    T v[kGenU];
+#pragma unroll
+    for (int u = 0; u < kGenU; ++u)
+      if (base + (int64_t)u * blockDim.x < g.n) v[u] = A[src[u]];
+#pragma unroll
+    for (int u = 0; u < kGenU; ++u)
+      if (base + (int64_t)u * blockDim.x < g.n) R[dst[u]] = v[u];
   }
 }
 
@@ -484,10 +528,27 @@ static int permute(const heal_tensor *a, const heal_tensor *perms, const heal_te
         g.f_ewmod = fastdiv_make((uint32_t)l);
       }
     }
-    if (r->dtype == HEAL_INT32)
-      permute_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
-    else
-      permute_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    if (!g.dense) {
+      // general path: merge the axes other than the two whose coordinates it reads
+      View *vs[2] = {&g.r, &g.a};
+      int map[HEAL_MAX_DIMS];
+      coalesce_views(vs, 2, (1u << ew) | (1u << pa), map);
+      g.ew = map[ew];
+      g.pa = map[pa];
+      make_fast_dims(g.r, n, &g.fd);
+    }
+    if (g.dense) {
+      if (r->dtype == HEAL_INT32)
+        permute_dense_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+      else
+        permute_dense_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
+    } else {
+      const int64_t work = (n + kGenU - 1) / kGenU;
+      if (r->dtype == HEAL_INT32)
+        permute_general_kernel<int32_t><<<grid_for(work, 256, 8), 256, 0, stream()>>>(g);
+      else
+        permute_general_kernel<int64_t><<<grid_for(work, 256, 8), 256, 0, stream()>>>(g);
+    }
     rc = check_launch("permute");
   }
   scratch_free(oa);

@@ -221,26 +221,54 @@ bool identical_view(const heal_tensor &a, const heal_tensor &b) {
 // ========================================================= strided gather
 struct CopyArgs {
   View src, dst;
+  FastDims fd;
   int64_t n;
   const char *s;
   char *d;
 };
 
+// kCopyU elements per thread per iteration, loads issued together
+constexpr int kCopyU = 4;
+
 template <typename W>
-__global__ void __launch_bounds__(256) copy_strided_kernel(CopyArgs a) {
+__global__ void __launch_bounds__(256) copy_strided_kernel(const __grid_constant__ CopyArgs a) {
   const W *src = (const W *)a.s;
   W *dst = (W *)a.d;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < a.n;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t rem = idx, so = 0, dofs = 0;
-    for (int i = a.dst.ndim - 1; i >= 0; --i) {
-      int64_t d = a.dst.dims[i];
-      int64_t c = rem % d;
-      rem /= d;
-      so += c * a.src.strides[i];
-      dofs += c * a.dst.strides[i];
+  const int64_t step = (int64_t)gridDim.x * blockDim.x * kCopyU;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * kCopyU + threadIdx.x; base < a.n; base += step) {
+    int64_t so[kCopyU], dofs[kCopyU];
+#pragma unroll
+    for (int u = 0; u < kCopyU; ++u) {
+      const int64_t idx = base + (int64_t)u * blockDim.x;
+      so[u] = dofs[u] = 0;
+      if (idx >= a.n) continue;
+      if (a.fd.fast) {
+        uint32_t rem = (uint32_t)idx;
+        for (int i = a.dst.ndim - 1; i >= 0; --i) {
+          const uint32_t q = fastdiv(rem, a.fd.fd[i]);
+          const int64_t c = rem - q * (uint32_t)a.dst.dims[i];
+          rem = q;
+          so[u] += c * a.src.strides[i];
+          dofs[u] += c * a.dst.strides[i];
+        }
+      } else {
+        int64_t rem = idx;
+        for (int i = a.dst.ndim - 1; i >= 0; --i) {
+          const int64_t d = a.dst.dims[i];
+          const int64_t c = rem % d;
+          rem /= d;
+          so[u] += c * a.src.strides[i];
+          dofs[u] += c * a.dst.strides[i];
+        }
+      }
     }
-    dst[dofs] = src[so];
+    W v[kCopyU];
+#pragma unroll
+    for (int u = 0; u < kCopyU; ++u)
+      if (base + (int64_t)u * blockDim.x < a.n) v[u] = src[so[u]];
+#pragma unroll
+    for (int u = 0; u < kCopyU; ++u)
+      if (base + (int64_t)u * blockDim.x < a.n) dst[dofs[u]] = v[u];
   }
 }
 
@@ -256,13 +284,17 @@ int copy_strided_impl(const heal_tensor &src, const heal_tensor &dst) {
   CopyArgs a;
   a.src = make_view(src);
   a.dst = make_view(dst);
+  View *vs[2] = {&a.src, &a.dst};
+  coalesce_views(vs, 2, 0u, nullptr);
+  make_fast_dims(a.dst, n, &a.fd);
   a.n = n;
   a.s = (const char *)src.data;
   a.d = (char *)dst.data;
+  const int64_t work = (n + kCopyU - 1) / kCopyU;
   if (elem_size(src.dtype) == 4)
-    copy_strided_kernel<uint32_t><<<grid_for(n, 256), 256, 0, stream()>>>(a);
+    copy_strided_kernel<uint32_t><<<grid_for(work, 256), 256, 0, stream()>>>(a);
   else
-    copy_strided_kernel<uint64_t><<<grid_for(n, 256), 256, 0, stream()>>>(a);
+    copy_strided_kernel<uint64_t><<<grid_for(work, 256), 256, 0, stream()>>>(a);
   HEAL_CHECK(check_launch("copy_strided"));
   mark_written(dst.data);
   return HEAL_OK;

@@ -1,0 +1,384 @@
+"""Serving loop: encrypted-vector x plaintext-matrix products on one GB300.
+
+A request multiplies a resident NTT-domain ciphertext ct[2, N, L] by a d x d
+plaintext matrix with the diagonal method: out = sum_i diag_i * rot_i(ct),
+where rot_i is the Galois automorphism X -> X^(5^i) (a permutation of the
+NTT-domain evaluation points) and diag_i is the i-th generalised diagonal of
+the matrix tiled over the N slots.  Three HEAL calls do it:
+
+  permute      ct expanded (stride 0) to [d, 2, N, L], rows of perms[d, N]
+               = the d Galois maps, elementwise axis 0, permuted axis 2
+               -> the rotated stack R[d, 2, N, L]
+  modmul       R viewed as [d, 2, N/d, d, L] times the diagonals
+               [d, 1, 1, d, L] (broadcast over both polynomials and the
+               N/d tiles), in place
+  axis_modsum  R over axis 0 -> out[2, N, L]
+
+with the matrix copied in (H2D, pinned) before and the result copied out
+(D2H, pinned) after, all on the request's stream.
+
+Scheduling.  Arrivals follow a seeded Poisson process.  A request is
+admitted, in arrival order, once its device footprint (rotated stack,
+diagonals, output) fits in a fixed HBM arena; the arena's host-side
+first-fit allocator hands out byte ranges of one heal_alloc buffer, and a
+range returns to it only after the request's completion event has fired, so
+no stream can still be using memory that another request receives.
+Admitted requests go round-robin over a set of CUDA streams.  Latency is
+completion (observed by polling the event) minus arrival.
+"""
+from __future__ import annotations
+
+import bisect
+import ctypes
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import params as P
+
+ALIGN = 256
+
+
+# ------------------------------------------------------------ host logic
+class Arena:
+    """First-fit allocator over [0, size) with coalescing of free ranges."""
+
+    def __init__(self, size: int):
+        self.size = size
+        self.free_list = [(0, size)]          # sorted, disjoint (offset, length)
+        self.live = {}
+        self.peak = 0
+
+    @property
+    def used(self) -> int:
+        return sum(self.live.values())
+
+    def alloc(self, nbytes: int):
+        n = max(ALIGN, (nbytes + ALIGN - 1) // ALIGN * ALIGN)
+        for i, (off, ln) in enumerate(self.free_list):
+            if ln >= n:
+                if ln == n:
+                    self.free_list.pop(i)
+                else:
+                    self.free_list[i] = (off + n, ln - n)
+                self.live[off] = n
+                self.peak = max(self.peak, self.used)
+                return off
+        return None
+
+    def free(self, off: int):
+        n = self.live.pop(off)
+        i = bisect.bisect(self.free_list, (off, 0))
+        self.free_list.insert(i, (off, n))
+        # merge with the neighbours
+        if i + 1 < len(self.free_list) and off + n == self.free_list[i + 1][0]:
+            self.free_list[i] = (off, n + self.free_list.pop(i + 1)[1])
+        if i > 0 and self.free_list[i - 1][0] + self.free_list[i - 1][1] == off:
+            po, pn = self.free_list[i - 1]
+            self.free_list[i - 1] = (po, pn + self.free_list.pop(i)[1])
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds from the start of the run
+    n: int
+    l: int
+    d: int
+    ct: int                 # resident ciphertext index for (n, l)
+    mat: int                # matrix variant for (d, l)
+    admitted: float = -1.0
+    done: float = -1.0
+
+    fused: bool = False
+
+    def footprint(self) -> int:
+        """Device bytes the request holds while in flight: the rotated stack
+        (or, fused, the diagonals tiled over the slots), the diagonals as
+        sent, and the output."""
+        first = full_diag_bytes(self.n, self.l, self.d) if self.fused else stack_bytes(self.n, self.l, self.d)
+        return first + diag_bytes(self.l, self.d) + out_bytes(self.n, self.l)
+
+
+def stack_bytes(n, l, d):
+    return d * 2 * n * l * 8
+
+
+def diag_bytes(l, d):
+    return d * d * l * 8
+
+
+def full_diag_bytes(n, l, d):
+    return d * n * l * 8
+
+
+def out_bytes(n, l):
+    return 2 * n * l * 8
+
+
+def poisson_schedule(count: int, rate: float, seed: int, ns, ds, lmin: int, lmax: int, cts: int, mats: int):
+    """`count` requests with exponential inter-arrival gaps of mean 1/rate;
+    ring degree, dimension, limb count, ciphertext and matrix are drawn
+    uniformly, all from SplitMix64 streams of `seed`."""
+    u = (P.splitmix64(seed, count) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+    gaps = -np.log1p(-u) / rate
+    t = np.cumsum(gaps)
+    pick = lambda s, lo, hi: P.uniform(seed + s, (count,), lo, hi)
+    ni, di, ls = pick(1, 0, len(ns)), pick(2, 0, len(ds)), pick(3, lmin, lmax + 1)
+    ci, mi = pick(4, 0, cts), pick(5, 0, mats)
+    return [Request(i, float(t[i]), int(ns[ni[i]]), int(ls[i]), int(ds[di[i]]), int(ci[i]), int(mi[i]))
+            for i in range(count)]
+
+
+@dataclass
+class LoopStats:
+    latencies: list = field(default_factory=list)
+    waits: list = field(default_factory=list)
+    max_queue: int = 0
+    max_inflight: int = 0
+    peak_bytes: int = 0
+    span: float = 0.0
+
+
+def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max_inflight: int = 64):
+    """Runs the admission loop.  issue(req, offset) enqueues the request's GPU
+    work and returns an object with query() -> bool (True once finished) and
+    finish() (called once, after query() turned True).  Requests are admitted
+    in arrival order when their footprint fits in the arena."""
+    pending = sorted(requests, key=lambda r: r.arrival)
+    queue, inflight, st = [], [], LoopStats()
+    nxt, t0 = 0, clock()
+    while nxt < len(pending) or queue or inflight:
+        now = clock() - t0
+        while nxt < len(pending) and pending[nxt].arrival <= now:
+            queue.append(pending[nxt])
+            nxt += 1
+        st.max_queue = max(st.max_queue, len(queue))
+        progressed = False
+        for item in list(inflight):
+            req, off, h = item
+            if h.query():
+                req.done = clock() - t0
+                h.finish()
+                arena.free(off)
+                inflight.remove(item)
+                st.latencies.append(req.done - req.arrival)
+                progressed = True
+        while queue and len(inflight) < max_inflight:
+            req = queue[0]
+            off = arena.alloc(req.footprint())
+            if off is None:
+                if not inflight:
+                    raise MemoryError(f"request {req.rid} needs {req.footprint()} bytes, more than the arena")
+                break
+            queue.pop(0)
+            req.admitted = clock() - t0
+            st.waits.append(req.admitted - req.arrival)
+            inflight.append((req, off, issue(req, off)))
+            progressed = True
+        st.max_inflight = max(st.max_inflight, len(inflight))
+        st.peak_bytes = max(st.peak_bytes, arena.used)
+        if not progressed and idle is not None:
+            idle()
+    st.span = (max(r.done for r in pending) - pending[0].arrival) if pending else 0.0
+    return st
+
+
+def percentile(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if xs else 0.0
+
+
+# ------------------------------------------------------------- the device
+class MatVecServer:
+    """Resident ciphertexts, rotation tables and the HBM arena for the
+    matrix-vector requests; `issue` runs one request on the next stream."""
+
+    def __init__(self, ns=(1 << 14, 1 << 15), ds=(16, 64, 256), lmin=8, lmax=16, bits=40, cts=2, mats=2,
+                 budget=16 << 30, streams=8, seed=505, fused=False):
+        import torch
+        from . import capi
+        self.capi, self.torch = capi, torch
+        self.ns, self.ds, self.lmin, self.lmax, self.cts, self.mats = ns, ds, lmin, lmax, cts, mats
+        self.fused = fused
+        D = capi.DeviceArray.from_numpy
+        self.qs = {n: P.ntt_primes(1 << bits, n, lmax) for n in ns}
+        self.p = {(n, l): D(np.array(self.qs[n][:l], np.int64)) for n in ns for l in range(lmin, lmax + 1)}
+        # resident NTT-domain ciphertexts, uniform mod q
+        self.ct = {(n, l): [D(P.residues(seed + 7919 * c + 31 * l + n, (2, n, l), self.qs[n][:l]))
+                            for c in range(cts)] for n in ns for l in range(lmin, lmax + 1)}
+        # Galois maps X -> X^(5^i), i < d, per ring degree
+        self.perms = {}
+        for n in ns:
+            for d in ds:
+                elts = [pow(5, i, 2 * n) for i in range(d)]
+                self.perms[(n, d)] = D(np.stack([P.galois_perm(n, e) for e in elts]).astype(np.int64))
+        # matrix diagonals [d, 1, 1, d, L] (uniform mod q), pinned for the H2D
+        self.host_mats = {}
+        for d in ds:
+            for l in range(lmin, lmax + 1):
+                for v in range(mats):
+                    self.host_mats[(d, l, v)] = {
+                        n: torch.from_numpy(P.residues(seed + 104729 * v + 613 * d + l + n, (d, 1, 1, d, l),
+                                                       self.qs[n][:l])).pin_memory() for n in ns}
+        self.arena_size = budget
+        self.arena_buf = capi.Buffer(budget, zero=False)
+        self.arena = Arena(budget)
+        self.streams = [torch.cuda.Stream() for _ in range(streams)]
+        self.rr = 0
+        self.out_host = {}
+        self.keep = set()                    # request ids whose output is kept
+
+    # views into the arena
+    def _view(self, off, shape):
+        return self.capi.DeviceArray(self.arena_buf, np.int64, shape, None, off)
+
+    def enqueue(self, req: Request, off: int, stream):
+        """Issues the request's copies and three HEAL calls on `stream`; the
+        output lands in a pinned host array returned with the event."""
+        capi, n, l, d = self.capi, req.n, req.l, req.d
+        capi.check(capi.lib().heal_set_stream(stream.cuda_stream))
+        try:
+            first = full_diag_bytes(n, l, d) if self.fused else stack_bytes(n, l, d)
+            o_stack, o_diag = off, off + first
+            o_out = o_diag + diag_bytes(l, d)
+            R = self._view(o_stack, (d, 2, n, l))
+            diag = self._view(o_diag, (d, 1, 1, d, l))
+            out = self._view(o_out, (2, n, l))
+            host = self.host_mats[(d, l, req.mat)][n]
+            capi.check(capi.lib().heal_h2d_async(ctypes.c_void_p(diag.ptr), ctypes.c_void_p(host.data_ptr()),
+                                                 diag_bytes(l, d)))
+            ct = self.ct[(n, l)][req.ct]
+            src = ct.reshape((1, 2, n, l)).expand(0, d)
+            p = self.p[(n, l)]
+            if self.fused:
+                # the diagonals tiled over the N slots ([d, N, L], one broadcast
+                # copy), then sum_i rot_i(ct) * diag_i in one fused call over
+                # S = [d, N, 2, L]: both polynomials of a slot read one diagonal value
+                full = self._view(o_stack, (d, n // d, d, l))
+                tiled = capi.DeviceArray(self.arena_buf, np.int64, (d, n // d, d, l), (d * l, 0, l, 1), o_diag)
+                capi.call("heal_copy_strided", tiled, full)
+                a = ct.reshape((1, 2, n, l)).moveaxis(1, 2).expand(0, d)
+                b = self._view(o_stack, (d, n, 1, l))
+                capi.call("heal_modmul_axis_sum", a, b, p, self.perms[(n, d)], 1, out.moveaxis(0, 1), 0)
+            else:
+                capi.call("heal_permute", src, self.perms[(n, d)], R, 0, 2)
+                R5 = self._view(o_stack, (d, 2, n // d, d, l))
+                capi.call("heal_modmul_ttt", R5, diag, p, R5)
+                capi.call("heal_axis_modsum", R, p, out, 0)
+            res = self.torch.empty((2, n, l), dtype=self.torch.int64, pin_memory=True)
+            capi.check(capi.lib().heal_d2h_async(ctypes.c_void_p(res.data_ptr()), ctypes.c_void_p(out.ptr),
+                                                 out_bytes(n, l)))
+            ev = self.torch.cuda.Event()
+            ev.record(stream)
+        finally:
+            capi.check(capi.lib().heal_set_stream(None))
+        return ev, res
+
+    def issue(self, req: Request, off: int):
+        stream = self.streams[self.rr % len(self.streams)]
+        self.rr += 1
+        ev, res = self.enqueue(req, off, stream)
+        server = self
+
+        class Handle:
+            def query(self):
+                return ev.query()
+
+            def finish(self):
+                if req.rid in server.keep:
+                    server.out_host[req.rid] = res.numpy().copy()
+        return Handle()
+
+    def split_ms(self, req: Request, reps: int = 5) -> dict:
+        """Median CUDA-event time of each HEAL call of the request (its
+        copies excluded), for the server's path."""
+        capi, torch, n, l, d = self.capi, self.torch, req.n, req.l, req.d
+        req.fused = self.fused
+        off = self.arena.alloc(req.footprint())
+        stream = self.streams[0]
+        capi.check(capi.lib().heal_set_stream(stream.cuda_stream))
+        try:
+            first = full_diag_bytes(n, l, d) if self.fused else stack_bytes(n, l, d)
+            o_diag = off + first
+            out = self._view(o_diag + diag_bytes(l, d), (2, n, l))
+            ct = self.ct[(n, l)][req.ct]
+            p = self.p[(n, l)]
+            if self.fused:
+                full = self._view(off, (d, n // d, d, l))
+                tiled = capi.DeviceArray(self.arena_buf, np.int64, (d, n // d, d, l), (d * l, 0, l, 1), o_diag)
+                a = ct.reshape((1, 2, n, l)).moveaxis(1, 2).expand(0, d)
+                b = self._view(off, (d, n, 1, l))
+                o = out.moveaxis(0, 1)
+                calls = {"tile_diagonals": lambda: capi.call("heal_copy_strided", tiled, full),
+                         "modmul_axis_sum": lambda: capi.call("heal_modmul_axis_sum", a, b, p, self.perms[(n, d)],
+                                                              1, o, 0)}
+            else:
+                R = self._view(off, (d, 2, n, l))
+                R5 = self._view(off, (d, 2, n // d, d, l))
+                diag = self._view(o_diag, (d, 1, 1, d, l))
+                src = ct.reshape((1, 2, n, l)).expand(0, d)
+                calls = {"permute": lambda: capi.call("heal_permute", src, self.perms[(n, d)], R, 0, 2),
+                         "modmul": lambda: capi.call("heal_modmul_ttt", R5, diag, p, R5),
+                         "axis_modsum": lambda: capi.call("heal_axis_modsum", R, p, out, 0)}
+            res = {}
+            for name, fn in calls.items():
+                ts = []
+                for _ in range(reps):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    fn()
+                    e1.record(stream)
+                    e1.synchronize()
+                    ts.append(e0.elapsed_time(e1))
+                res[name] = sorted(ts)[len(ts) // 2]
+            return res
+        finally:
+            capi.check(capi.lib().heal_set_stream(None))
+            self.arena.free(off)
+
+    def alone(self, req: Request) -> np.ndarray:
+        """The request run by itself (one stream, nothing else in flight)."""
+        req.fused = self.fused
+        off = self.arena.alloc(req.footprint())
+        if off is None:
+            raise MemoryError("arena full")
+        try:
+            ev, res = self.enqueue(req, off, self.streams[0])
+            ev.synchronize()
+            return res.numpy().copy()
+        finally:
+            self.arena.free(off)
+
+    def warm(self):
+        """One request of every (n, l, d) shape, so that every table the
+        calls derive is cached before timing."""
+        rid = -1
+        for n in self.ns:
+            for l in range(self.lmin, self.lmax + 1):
+                for d in self.ds:
+                    self.alone(Request(rid, 0.0, n, l, d, 0, 0))
+        self.torch.cuda.synchronize()
+
+    def run(self, requests, keep=()):
+        for r in requests:
+            r.fused = self.fused
+        self.keep = set(keep)
+        self.out_host = {}
+        return serve(requests, self.arena, self.issue)
+
+    @staticmethod
+    def bytes_moved(req: Request) -> int:
+        """Algorithmic bytes of one request, copies to and from the host
+        included.  Three calls: permute writes the stack (the ciphertext is
+        read once per rotation, from L2), modmul reads it and writes it,
+        axis_modsum reads it and writes the output.  Fused: the tiling copy
+        writes the full diagonals, modmul_axis_sum reads them once and the
+        ciphertext once and writes the output."""
+        n, l, d = req.n, req.l, req.d
+        io = 2 * diag_bytes(l, d) + 2 * out_bytes(n, l)   # H2D + its read, D2H + its write
+        if req.fused:
+            f = full_diag_bytes(n, l, d)
+            return 2 * f + out_bytes(n, l) + io
+        s = stack_bytes(n, l, d)
+        return 4 * s + io

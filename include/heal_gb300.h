@@ -250,6 +250,20 @@ int heal_ntt_autotune(int inverse, const heal_tensor *a, const heal_tensor *p, c
 int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tensor *result, int64_t elementwise_axis,
                  int64_t perm_axis);
 
+/* Fused multiply-reduce, the backend op behind HEAL's DeviceDispatcher
+ * modmul_axis_sum (python_execution/lattica_heal_runtime/device_interface.py:
+ * 67-68, which names the op only).  Defined as the composition
+ *   result = axis_modsum(modmul(a', b, p), axis)
+ * with a and b broadcast like modmul to a common shape S (result's shape with
+ * `axis` re-inserted; axis in [0, ndim(S) - 2]; p of shape [S[-1]]), and
+ * a' = a when perms is NULL, else a gathered like permute with
+ * elementwise_axis = axis: a'[c] = a[c with c[perm_axis] <- perms[c[axis],
+ * c[perm_axis]]], perms of shape [S[axis], S[perm_axis]].  Bit-identical to
+ * the separate calls; the product is never written.  Errors as axis_modsum /
+ * permute. */
+int heal_modmul_axis_sum(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
+                         int64_t perm_axis, const heal_tensor *result, int64_t axis);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

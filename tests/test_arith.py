@@ -86,3 +86,14 @@ def test_fastdiv(harness):
             rows.append(("fastdiv", n, 0, d))
             want.append(n // d)
     assert run(harness, rows) == want
+
+
+def test_view_coalescing(tmp_path):
+    """heal_view.h: merged views address every element exactly as the
+    original views do (64-bit and FastDiv decomposition), kept axes keep
+    their coordinates."""
+    exe = str(tmp_path / "view_check")
+    subprocess.run(["g++", "-std=c++17", "-O2", os.path.join(HERE, "native", "view_check.cpp"), "-o", exe],
+                   check=True)
+    out = subprocess.run([exe], capture_output=True, text=True).stdout.strip()
+    assert out == "ok 20000", out

@@ -1,0 +1,43 @@
+"""Serving loop on the GPU at reduced sizes: every request of a burst that
+the arena budget forces to queue gives the oracle's
+permute -> modmul -> axis_modsum result, and the same result as when the
+request runs alone."""
+import numpy as np
+import pytest
+
+from heal_gb300 import serving as S
+from oracle import oracle as O
+from _gpu import ready
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def gpu():
+    return ready()
+
+
+def oracle_product(srv, req):
+    n, l, d = req.n, req.l, req.d
+    ct = srv.ct[(n, l)][req.ct].numpy()
+    perms = srv.perms[(n, d)].numpy()
+    diag = srv.host_mats[(d, l, req.mat)][n].numpy()
+    p = np.array(srv.qs[n][:l], np.int64)
+    stack = O.permute(np.ascontiguousarray(np.broadcast_to(ct[None], (d, 2, n, l))), perms, 0, 2)
+    prod = O.modmul(stack.reshape(d, 2, n // d, d, l), diag, p)
+    return O.axis_modsum(prod.reshape(d, 2, n, l), p, 0)
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_serving_outputs_match_oracle_and_standalone(fused):
+    srv = S.MatVecServer(ns=(256, 512), ds=(2, 4, 8), lmin=2, lmax=4, bits=40, cts=2, mats=2,
+                         budget=1 << 20, streams=3, seed=21, fused=fused)
+    srv.warm()
+    reqs = S.poisson_schedule(60, 50000.0, 8, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
+    st = srv.run(reqs, keep=[r.rid for r in reqs])
+    assert len(st.latencies) == len(reqs) and st.max_queue > 1 and st.max_inflight > 1
+    assert st.peak_bytes <= 1 << 20
+    for r in reqs:
+        got = srv.out_host[r.rid]
+        assert np.array_equal(got, oracle_product(srv, r)), r
+        assert np.array_equal(got, srv.alone(r)), r
