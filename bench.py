@@ -53,6 +53,23 @@ def dist_info():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's time (every rank gets it); a no-op on one rank."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, ms: float) -> float:
+    """Units all ranks processed per second, over the slowest rank's time
+    (each rank runs its own replicas: weak scaling)."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 class Clocks:
     """Samples SM clocks and throttle reasons with nvidia-smi while running."""
 
@@ -215,11 +232,7 @@ def our_arm(args):
         stop.record(stream)
         stop.synchronize()
         barrier()
-        ms = start.elapsed_time(stop)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(start.elapsed_time(stop), world, "cuda")
         return ms, capi.launches() - l0
 
     # ---- correctness of the timed configuration (one step, spot-checked)
@@ -230,7 +243,7 @@ def our_arm(args):
     with Clocks(local) as clk:
         ms, launches = timed(chain_step, args.steps)
     clocks = clk.summary()
-    value = args.steps * world / (ms / 1e3)
+    value = whole_job_rate(args.steps, world, ms)
 
     # ---- batched NTT of the digits (the dominant kernel) and the per-call split
     ntt_step = lambda s: capi.call("heal_ntt", ch.dig_flat, ch.dev["p_t"], ch.dev["perm"], ch.dev["tw_t"],
@@ -283,7 +296,7 @@ def our_arm(args):
     for w in range(args.warmup):
         e2e_step(w)
     e2e_ms, _ = timed(e2e_step, args.steps)
-    e2e = args.steps * world / (e2e_ms / 1e3)
+    e2e = whole_job_rate(args.steps, world, e2e_ms)
     got = np.frombuffer((ctypes.c_char * nbytes).from_address(pin_out.value), dtype=np.int64).reshape(ch.shape())
     want = outs[0].numpy()
     assert np.array_equal(got, want), "e2e output differs from the resident run"
