@@ -497,6 +497,24 @@ def serve_once(count, rate, fused):
     return res
 
 
+def request_probe(args):
+    """--mode request: one serving request (d = --d, N = --n, L = 16) on a
+    one-shape server, each of its calls timed with CUDA events; for ncu
+    captures of the serving kernels.  --fused selects the fused path."""
+    import heal_gb300
+    from heal_gb300 import capi
+    from heal_gb300 import serving as S
+    heal_gb300.build()
+    capi.check(capi.lib().heal_init(0))
+    srv = S.MatVecServer(ns=(args.n,), ds=(args.d,), lmin=16, lmax=16, cts=1, mats=1, budget=4 << 30, streams=1,
+                         fused=args.fused)
+    srv.warm()
+    r = S.Request(-1, 0.0, args.n, 16, args.d, 0, 0)
+    print(json.dumps({"mode": "request", "d": args.d, "n": args.n, "fused": args.fused,
+                      "split_ms": srv.split_ms(r, reps=3)}), flush=True)
+    return 0
+
+
 def ntt_probe(args):
     """--mode ntt: one batched NTT alone, for ncu captures of the pass
     kernels.  --probe digits: [batch, 65536, 1, 72] int64 under the chain's
@@ -552,7 +570,10 @@ def main():
     ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--configs", default="cfg1,cfg3,cfg4,cfg5",
                     help="comma-separated configurations reported beside the headline")
-    ap.add_argument("--mode", default="chain", choices=["chain", "ntt"])
+    ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request"])
+    ap.add_argument("--d", type=int, default=64, help="--mode request: matrix dimension")
+    ap.add_argument("--n", type=int, default=1 << 14, help="--mode request: ring degree")
+    ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--probe", default="digits", choices=["digits", "cfg4"])
     args = ap.parse_args()
@@ -560,6 +581,8 @@ def main():
         args.warmup = 3
     if args.mode == "ntt":
         return ntt_probe(args)
+    if args.mode == "request":
+        return request_probe(args)
     if args.impl == "reference":
         return reference_arm(args)
     return our_arm(args)

@@ -8,7 +8,10 @@
 // with a and b broadcast like modmul (example_impl/modop_impl.cpp:44-101) to
 // a common shape S, and a' = a or, with `perms`, a gathered like permute
 // with elementwise_axis = axis (example_impl/permute_impl.cpp:8-65):
-// a'[c] = a[c with c[perm_axis] <- perms[c[axis], c[perm_axis]]].
+// a'[c] = a[c with c[perm_axis] <- perms[c[axis], c[perm_axis]]].  A perms
+// tensor with one more axis, [S[axis], S[pa], S[pa+1]], gathers over the two
+// axes pa, pa+1 taken as one flattened axis (a linear across them): the same
+// as permute on a with those two axes reshaped into one.
 // The product is never written: one thread per result element runs the
 // reduction, so a rotate-multiply-accumulate over d rotations reads the
 // rotated operand (resident in L2) and b once and writes only the result.
@@ -34,10 +37,11 @@ struct FusedArgs {
   View ao, bo;            // a and b strides in result coordinates
   int64_t a_ax, b_ax;     // strides along the reduced axis
   int64_t len;            // reduced length
-  int pa;                 // perm axis in result coordinates, -1 without perms
+  int pa, pa2;            // gathered axes in result coordinates (-1: none)
   int last;               // last axis in result coordinates
-  int64_t a_pa;           // a's stride along the perm axis
-  int64_t ps0, ps1;       // perms strides
+  int64_t a_pa;           // a's stride along the (innermost) gathered axis
+  int64_t ps0, ps1;       // perms strides: reduced axis, flattened gathered index
+  int gather32;           // every gathered offset index * a_pa fits in 31 bits
   const void *a, *b, *perms;
   int perms_dtype;
   const void *ptab;       // MG64 / MG32 per modulus
@@ -51,9 +55,9 @@ template <typename T> struct FusedMG;
 template <> struct FusedMG<int32_t> { typedef MG32 type; };
 template <> struct FusedMG<int64_t> { typedef MG64 type; };
 
+template <typename PT>
 __device__ __forceinline__ int64_t fused_perm(const FusedArgs &g, int64_t i, int64_t c) {
-  return g.perms_dtype == HEAL_INT32 ? (int64_t)((const int32_t *)g.perms)[i * g.ps0 + c * g.ps1]
-                                     : ((const int64_t *)g.perms)[i * g.ps0 + c * g.ps1];
+  return (int64_t)((const PT *)g.perms)[i * g.ps0 + c * g.ps1];
 }
 
 // one term's element of modmul then one step of axis_modsum's running sum,
@@ -75,17 +79,23 @@ __device__ __forceinline__ int64_t exact_step(int64_t sum, int64_t a, int64_t b,
   return crem128((i128)sum + (i128)v, q);
 }
 
-constexpr int kFusedU = 4;
+// terms per batch of the reduction loop
+#ifndef HEAL_FUSED_U
+#define HEAL_FUSED_U 4
+#endif
+constexpr int kFusedU = HEAL_FUSED_U;
 
-template <typename T>
+template <typename T, typename PT, typename Off>
 __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_constant__ FusedArgs g) {
   typedef typename FusedMG<T>::type M;
   const T *A = (const T *)g.a;
   const T *B = (const T *)g.b;
+  const PT *PP = (const PT *)g.perms;
   T *R = (T *)g.out;
+  const Off a_ax = (Off)g.a_ax, b_ax = (Off)g.b_ax, ps0 = (Off)g.ps0;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t a0 = 0, b0 = 0, r0 = 0, t = 0, cp = 0;
+    int64_t a0 = 0, b0 = 0, r0 = 0, t = 0, cp = 0, cp2 = 0;
     if (g.fd.fast) {
       uint32_t rem = (uint32_t)idx;
       for (int i = g.r.ndim - 1; i >= 0; --i) {
@@ -94,6 +104,7 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
         rem = qd;
         if (i == g.last) t = c;
         if (i == g.pa) cp = c;
+        if (i == g.pa2) cp2 = c;
         a0 += c * g.ao.strides[i];
         b0 += c * g.bo.strides[i];
         r0 += c * g.r.strides[i];
@@ -105,11 +116,13 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
         rem /= g.r.dims[i];
         if (i == g.last) t = c;
         if (i == g.pa) cp = c;
+        if (i == g.pa2) cp2 = c;
         a0 += c * g.ao.strides[i];
         b0 += c * g.bo.strides[i];
         r0 += c * g.r.strides[i];
       }
     }
+    if (g.pa2 >= 0) cp = cp * g.r.dims[g.pa2] + cp2;  // flattened index over the gathered pair
     const M mc = ((const M *)g.ptab)[t];
     const int64_t q = sizeof(T) == 4 ? (int64_t)(int32_t)((const MG32 &)mc).q : (int64_t)((const MG64 &)mc).q;
     if (q == 0) {  // modmul and axis_modsum both give 0 for a zero modulus
@@ -118,47 +131,69 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
       continue;
     }
     const bool perm = g.pa >= 0;
+    const uint64_t uq = (uint64_t)q, q32 = uq << 32;
+    // Admission of the fast path.  For non-negative terms the composition is
+    // (sum of products) mod q whatever their size; with 64-bit words and
+    // q < 2^62, terms below 2^bitlen(q) keep the accumulator's high word below
+    // q, so OR-ing every term and testing the high bits once suffices.
+    // Otherwise (32-bit words, larger q) every term is compared with q.
+    const bool orcheck = sizeof(T) == 8 && q > 0 && q < ((int64_t)1 << 62);
+    const uint64_t himask = orcheck ? ~((uint64_t(1) << (64 - __clzll(q))) - 1) : 0;
+    uint64_t ormask = 0;
     bool canon = q > 0;
     uint64_t hi = 0, lo = 0;  // 64-bit words: hi * 2^64 + lo, hi < q; 32-bit words: lo < q * 2^32
-    const uint64_t uq = (uint64_t)q, q32 = uq << 32;
-    for (int64_t i0 = 0; i0 < g.len && canon; i0 += kFusedU) {
-      int64_t aoff[kFusedU];
+    auto mac = [&](uint64_t x, uint64_t y) {
+      if (orcheck) ormask |= x | y;
+      else canon = canon && x < uq && y < uq;  // also rejects negative values
+      if (sizeof(T) == 4) {
+        lo += x * y;                            // < 2 q 2^32 < 2^64
+        lo = lo >= q32 ? lo - q32 : lo;
+      } else {
+        const uint64_t plo = x * y, phi = mulhi64(x, y);
+        const uint64_t s = lo + plo;
+        hi += phi + (s < lo ? 1 : 0);           // < 2q
+        lo = s;
+        hi = hi >= uq ? hi - uq : hi;
+      }
+    };
+    // kFusedU terms per batch through running offsets; the permutation
+    // indices of the next batch are fetched while this batch's operands load
+    Off ai = (Off)a0, bi = (Off)b0, pi = perm ? (Off)(cp * g.ps1) : (Off)0;
+    auto gather = [&](Off v) -> Off { return g.gather32 ? (Off)((int32_t)v * (int32_t)g.a_pa) : v * (Off)g.a_pa; };
+    Off pidx[kFusedU];
+#pragma unroll
+    for (int u = 0; u < kFusedU; ++u) pidx[u] = (perm && u < g.len) ? (Off)PP[pi + u * ps0] : (Off)0;
+    int64_t i0 = 0;
+    for (; i0 + kFusedU <= g.len && (orcheck || canon); i0 += kFusedU) {
+      uint64_t av[kFusedU], bv[kFusedU];
 #pragma unroll
       for (int u = 0; u < kFusedU; ++u) {
-        const int64_t i = i0 + u < g.len ? i0 + u : i0;
-        aoff[u] = a0 + i * g.a_ax + (perm ? fused_perm(g, i, cp) * g.a_pa : 0);
+        av[u] = (uint64_t)(int64_t)A[ai + u * a_ax + gather(pidx[u])];
+        bv[u] = (uint64_t)(int64_t)B[bi + u * b_ax];
       }
-      int64_t av[kFusedU], bv[kFusedU];
+      ai += kFusedU * a_ax;
+      bi += kFusedU * b_ax;
+      if (perm) {
+        pi += kFusedU * ps0;
 #pragma unroll
-      for (int u = 0; u < kFusedU; ++u) {
-        const int64_t i = i0 + u < g.len ? i0 + u : i0;
-        av[u] = (int64_t)A[aoff[u]];
-        bv[u] = (int64_t)B[b0 + i * g.b_ax];
+        for (int u = 0; u < kFusedU; ++u) pidx[u] = i0 + kFusedU + u < g.len ? (Off)PP[pi + u * ps0] : (Off)0;
       }
 #pragma unroll
-      for (int u = 0; u < kFusedU; ++u) {
-        if (i0 + u >= g.len) break;
-        const uint64_t x = (uint64_t)av[u], y = (uint64_t)bv[u];
-        canon = canon && x < uq && y < uq;  // also rejects negative values
-        if (sizeof(T) == 4) {
-          lo += x * y;                      // < 2 q 2^32 < 2^64
-          lo = lo >= q32 ? lo - q32 : lo;
-        } else {
-          const uint64_t plo = x * y, phi = mulhi64(x, y);
-          const uint64_t s = lo + plo;
-          hi += phi + (s < lo ? 1 : 0);     // < 2q
-          lo = s;
-          hi = hi >= uq ? hi - uq : hi;
-        }
-      }
+      for (int u = 0; u < kFusedU; ++u) mac(av[u], bv[u]);
     }
+#pragma unroll
+    for (int u = 0; u < kFusedU; ++u) {  // the last len % kFusedU terms
+      if (i0 + u >= g.len) break;
+      mac((uint64_t)(int64_t)A[ai + u * a_ax + gather(pidx[u])], (uint64_t)(int64_t)B[bi + u * b_ax]);
+    }
+    if (orcheck) canon = (ormask & himask) == 0;
     int64_t res;
     if (canon) {
       res = sizeof(T) == 4 ? (int64_t)mg32_mod(lo, (const MG32 &)mc) : (int64_t)mg64_mod(hi, lo, (const MG64 &)mc);
     } else {
       res = 0;
       for (int64_t i = 0; i < g.len; ++i) {
-        const int64_t aoffs = a0 + i * g.a_ax + (perm ? fused_perm(g, i, cp) * g.a_pa : 0);
+        const int64_t aoffs = a0 + i * g.a_ax + (perm ? fused_perm<PT>(g, i, cp) * g.a_pa : 0);
         res = exact_step<T>(res, (int64_t)A[aoffs], (int64_t)B[b0 + i * g.b_ax], q, mc);
       }
     }
@@ -200,21 +235,43 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
     if (r->dims[j++] != S[i])
       return set_error(HEAL_ERR_INVALID_ARGUMENT, "Result must have the shape of a and b with the reduced axis removed.");
   }
+  // gathered axes: one (perms [l, m], as permute) or a pair taken as one
+  // flattened axis (perms [l, m1, m2], linear across its last two axes)
+  const int gp = perms ? perms->ndim - 1 : 0;
+  int64_t mflat = 0;
   if (perms) {
-    if (perm_axis < 0 || perm_axis >= nd) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Axis out of bounds.");
-    if (perm_axis == axis) return set_error(HEAL_ERR_INVALID_ARGUMENT, "axis and perm_axis must be different.");
-    if (perms->ndim != 2 || perms->dims[0] != S[axis] || perms->dims[1] != S[perm_axis])
+    if (gp < 1 || gp > 2)
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "Perms must have shape [l, m] (or [l, m1, m2] for two axes).");
+    if (perm_axis < 0 || perm_axis + gp > nd) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Axis out of bounds.");
+    if (axis >= perm_axis && axis < perm_axis + gp)
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "axis and perm_axis must be different.");
+    bool shape_ok = perms->dims[0] == S[axis];
+    mflat = 1;
+    for (int k = 0; k < gp; ++k) {
+      shape_ok = shape_ok && perms->dims[1 + k] == S[perm_axis + k];
+      mflat *= S[perm_axis + k];
+    }
+    if (!shape_ok)
       return set_error(HEAL_ERR_INVALID_ARGUMENT,
                        "Perms must have shape [l, m] where l and m match the shape at axis and perm_axis.");
+    if (gp == 2 && perms->dims[2] > 1 && perms->strides[1] != perms->strides[2] * perms->dims[2])
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "Perms must be linear across its last two axes.");
   }
   const int64_t n = numel(*r);
   if (n == 0) return HEAL_OK;
+  heal_tensor PV;  // perms as [l, m1 * m2]
+  if (perms) {
+    PV = *perms;
+    PV.ndim = 2;
+    PV.dims[1] = mflat;
+    PV.strides[1] = (gp == 2 && perms->dims[2] == 1) ? perms->strides[1] : perms->strides[gp];
+  }
   if (perms && S[axis] > 0) {
     bool valid = false;
-    HEAL_CHECK(perms_valid(*perms, S[perm_axis], &valid));
+    HEAL_CHECK(perms_valid(PV, mflat, &valid));
     if (!valid) return set_error(HEAL_ERR_OUT_OF_RANGE, "Permutation index out of bounds.");
   }
-  heal_tensor A = *a, B = *b, P = *p, PR = perms ? *perms : heal_tensor();
+  heal_tensor A = *a, B = *b, P = *p, PR = perms ? PV : heal_tensor();
   void *owned[4] = {nullptr, nullptr, nullptr, nullptr};
   auto detach = [&](heal_tensor &t, int slot) -> int {
     return overlaps(t, *r) ? materialize(t, &t, &owned[slot]) : HEAL_OK;
@@ -225,9 +282,9 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
   if (!rc && perms) rc = detach(PR, 3);
   ModTable mt;
   if (!rc) rc = mod_table(P, &mt);
+  FusedArgs g;
+  memset(&g, 0, sizeof g);
   if (!rc) {
-    FusedArgs g;
-    memset(&g, 0, sizeof g);
     // strides of a and b in S coordinates (0 on broadcast axes)
     int64_t as[HEAL_MAX_DIMS], bs[HEAL_MAX_DIMS];
     for (int i = 0; i < nd; ++i) {
@@ -235,47 +292,78 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
       as[i] = (ia >= 0 && A.dims[ia] != 1) ? A.strides[ia] : 0;
       bs[i] = (ib >= 0 && B.dims[ib] != 1) ? B.strides[ib] : 0;
     }
-    g.r = make_view(*r);
-    g.ao = g.r;
-    g.bo = g.r;
-    for (int i = 0, j = 0; i < nd; ++i) {
-      if (i == axis) continue;
-      g.ao.strides[j] = (perms && i == perm_axis) ? 0 : as[i];
-      g.bo.strides[j] = bs[i];
-      ++j;
+    if (gp == 2 && S[perm_axis + 1] > 1 && as[perm_axis] != as[perm_axis + 1] * S[perm_axis + 1]) {
+      rc = set_error(HEAL_ERR_INVALID_ARGUMENT, "a must be linear across the two gathered axes.");
+    } else {
+      g.r = make_view(*r);
+      g.ao = g.r;
+      g.bo = g.r;
+      for (int i = 0, j = 0; i < nd; ++i) {
+        if (i == axis) continue;
+        const bool gathered = perms && i >= perm_axis && i < perm_axis + gp;
+        g.ao.strides[j] = gathered ? 0 : as[i];
+        g.bo.strides[j] = bs[i];
+        ++j;
+      }
+      g.a_ax = as[axis];
+      g.b_ax = bs[axis];
+      g.len = S[axis];
+      // stride of the flattened gathered index: the inner axis's (the outer's if the inner has length 1)
+      g.a_pa = !perms ? 0 : (gp == 2 && S[perm_axis + 1] == 1) ? as[perm_axis] : as[perm_axis + gp - 1];
+      const int pa = perms ? (int)(perm_axis < axis ? perm_axis : perm_axis - 1) : -1;
+      const int last = nd - 2;
+      // merge axes other than the ones whose coordinates the kernel reads
+      unsigned keep = 1u << last;
+      if (pa >= 0) keep |= 1u << pa;
+      if (gp == 2) keep |= 1u << (pa + 1);
+      View *vs[3] = {&g.r, &g.ao, &g.bo};
+      int map[HEAL_MAX_DIMS];
+      coalesce_views(vs, 3, keep, map);
+      g.pa = pa >= 0 ? map[pa] : -1;
+      g.pa2 = gp == 2 ? map[pa + 1] : -1;
+      g.last = map[last];
+      make_fast_dims(g.r, n, &g.fd);
+      g.ps0 = perms ? PR.strides[0] : 0;
+      g.ps1 = perms ? PR.strides[1] : 0;
+      // indices are validated to lie in [0, mflat)
+      g.gather32 = perms && g.a_pa >= 0 && mflat > 0 &&
+                   (__int128)g.a_pa * (__int128)(mflat - 1) < ((__int128)1 << 31);
+      g.a = A.data;
+      g.b = B.data;
+      g.perms = perms ? PR.data : nullptr;
+      g.perms_dtype = perms ? PR.dtype : HEAL_INT64;
+      g.ptab = mt.consts;
+      g.out = r->data;
+      g.n = n;
+      g.diag = diag_device();
     }
-    g.a_ax = as[axis];
-    g.b_ax = bs[axis];
-    g.len = S[axis];
-    g.a_pa = perms ? as[perm_axis] : 0;
-    int pa = perms ? (int)(perm_axis < axis ? perm_axis : perm_axis - 1) : -1;
-    int last = nd - 2;
-    // merge axes other than the two whose coordinates the kernel reads
-    unsigned keep = 1u << last;
-    if (pa >= 0) keep |= 1u << pa;
-    View *vs[3] = {&g.r, &g.ao, &g.bo};
-    int map[HEAL_MAX_DIMS];
-    coalesce_views(vs, 3, keep, map);
-    g.pa = pa >= 0 ? map[pa] : -1;
-    g.last = map[last];
-    make_fast_dims(g.r, n, &g.fd);
-    g.ps0 = perms ? PR.strides[0] : 0;
-    g.ps1 = perms ? PR.strides[1] : 0;
-    g.a = A.data;
-    g.b = B.data;
-    g.perms = perms ? PR.data : nullptr;
-    g.perms_dtype = perms ? PR.dtype : HEAL_INT64;
-    g.ptab = mt.consts;
-    g.out = r->data;
-    g.n = n;
-    g.diag = diag_device();
+  }
+  // 32-bit running offsets when every operand spans fewer than 2^31 elements
+  auto span_ok = [](const heal_tensor &t) {
+    __int128 s = 0;
+    for (int i = 0; i < t.ndim; ++i) s += (__int128)(t.dims[i] > 0 ? t.dims[i] - 1 : 0) * (t.strides[i] < 0 ? -t.strides[i] : t.strides[i]);
+    return s < ((__int128)1 << 31) - 1;
+  };
+  const bool off32 = span_ok(A) && span_ok(B) && (!perms || span_ok(PR)) && g.a_ax >= 0 && g.b_ax >= 0 &&
+                     g.ps0 >= 0 && g.ps1 >= 0 && g.a_pa >= 0;
+  if (!rc) {
     const int threads = 256;
     const int64_t want = (n + threads - 1) / threads;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * 16));
-    if (dt == HEAL_INT32)
-      modmul_axis_sum_kernel<int32_t><<<grid, threads, 0, stream()>>>(g);
-    else
-      modmul_axis_sum_kernel<int64_t><<<grid, threads, 0, stream()>>>(g);
+    const bool p32 = g.perms_dtype == HEAL_INT32;
+    auto go = [&](auto t_tag, auto p_tag) {
+      typedef decltype(t_tag) TT;
+      typedef decltype(p_tag) PTT;
+      if (off32) modmul_axis_sum_kernel<TT, PTT, int32_t><<<grid, threads, 0, stream()>>>(g);
+      else modmul_axis_sum_kernel<TT, PTT, int64_t><<<grid, threads, 0, stream()>>>(g);
+    };
+    if (dt == HEAL_INT32) {
+      if (p32) go(int32_t(), int32_t());
+      else go(int32_t(), int64_t());
+    } else {
+      if (p32) go(int64_t(), int32_t());
+      else go(int64_t(), int64_t());
+    }
     rc = check_launch("modmul_axis_sum");
   }
   for (void *o : owned) scratch_free(o);

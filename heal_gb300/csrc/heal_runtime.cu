@@ -290,11 +290,30 @@ int copy_strided_impl(const heal_tensor &src, const heal_tensor &dst) {
   a.n = n;
   a.s = (const char *)src.data;
   a.d = (char *)dst.data;
-  const int64_t work = (n + kCopyU - 1) / kCopyU;
-  if (elem_size(src.dtype) == 4)
-    copy_strided_kernel<uint32_t><<<grid_for(work, 256), 256, 0, stream()>>>(a);
-  else
-    copy_strided_kernel<uint64_t><<<grid_for(work, 256), 256, 0, stream()>>>(a);
+  // 16-byte vectors when both innermost axes are unit-stride rows of whole,
+  // aligned vectors: the same kernel then moves one vector per index
+  const int es = elem_size(src.dtype), vec = 16 / es;
+  const int in = a.dst.ndim - 1;
+  bool v16 = ((uintptr_t)a.s % 16 == 0) && ((uintptr_t)a.d % 16 == 0) && a.src.strides[in] == 1 &&
+             a.dst.strides[in] == 1 && a.dst.dims[in] % vec == 0;
+  for (int i = 0; i < in && v16; ++i) v16 = a.src.strides[i] % vec == 0 && a.dst.strides[i] % vec == 0;
+  if (v16) {
+    a.dst.dims[in] /= vec;
+    a.src.dims[in] = a.dst.dims[in];
+    for (int i = 0; i < in; ++i) {
+      a.src.strides[i] /= vec;
+      a.dst.strides[i] /= vec;
+    }
+    a.n = n / vec;
+    make_fast_dims(a.dst, a.n, &a.fd);
+    copy_strided_kernel<uint4><<<grid_for((a.n + kCopyU - 1) / kCopyU, 256), 256, 0, stream()>>>(a);
+  } else {
+    const int64_t work = (n + kCopyU - 1) / kCopyU;
+    if (es == 4)
+      copy_strided_kernel<uint32_t><<<grid_for(work, 256), 256, 0, stream()>>>(a);
+    else
+      copy_strided_kernel<uint64_t><<<grid_for(work, 256), 256, 0, stream()>>>(a);
+  }
   HEAL_CHECK(check_launch("copy_strided"));
   mark_written(dst.data);
   return HEAL_OK;

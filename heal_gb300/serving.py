@@ -15,7 +15,10 @@ the matrix tiled over the N slots.  Three HEAL calls do it:
   axis_modsum  R over axis 0 -> out[2, N, L]
 
 with the matrix copied in (H2D, pinned) before and the result copied out
-(D2H, pinned) after, all on the request's stream.
+(D2H, pinned) after, all on the request's stream.  The fused path does the
+same in one heal_modmul_axis_sum over S = [d, N/d, d, 2, L] (slot j = u*d + s):
+the ciphertext and the d x d diagonals enter as stride-only views and the
+rotation gathers over the flattened slot pair, so no stack is written.
 
 Scheduling.  Arrivals follow a seeded Poisson process.  A request is
 admitted, in arrival order, once its device footprint (rotated stack,
@@ -95,10 +98,9 @@ class Request:
 
     def footprint(self) -> int:
         """Device bytes the request holds while in flight: the rotated stack
-        (or, fused, the diagonals tiled over the slots), the diagonals as
-        sent, and the output."""
-        first = full_diag_bytes(self.n, self.l, self.d) if self.fused else stack_bytes(self.n, self.l, self.d)
-        return first + diag_bytes(self.l, self.d) + out_bytes(self.n, self.l)
+        (three calls only), the diagonals as sent, and the output."""
+        stack = 0 if self.fused else stack_bytes(self.n, self.l, self.d)
+        return stack + diag_bytes(self.l, self.d) + out_bytes(self.n, self.l)
 
 
 def stack_bytes(n, l, d):
@@ -107,10 +109,6 @@ def stack_bytes(n, l, d):
 
 def diag_bytes(l, d):
     return d * d * l * 8
-
-
-def full_diag_bytes(n, l, d):
-    return d * n * l * 8
 
 
 def out_bytes(n, l):
@@ -233,39 +231,46 @@ class MatVecServer:
     def _view(self, off, shape):
         return self.capi.DeviceArray(self.arena_buf, np.int64, shape, None, off)
 
+    def calls(self, req: Request, off: int) -> dict:
+        """The request's HEAL calls (name -> thunk) on its arena range at
+        `off`, in order: the rotated stack, the diagonal product and the sum
+        (three calls), or one modmul_axis_sum (fused)."""
+        capi, n, l, d = self.capi, req.n, req.l, req.d
+        o_diag = off if self.fused else off + stack_bytes(n, l, d)
+        out = self._view(o_diag + diag_bytes(l, d), (2, n, l))
+        ct = self.ct[(n, l)][req.ct]
+        p, perms = self.p[(n, l)], self.perms[(n, d)]
+        if self.fused:
+            # S = [d, N/d, d, 2, L] over (i, u, s, c, t), slot j = u * d + s:
+            # a = ct (stride 0 on i), b = diag[i, s, t] (broadcast over u and c),
+            # the rotation gathers over the flattened slot pair (u, s)
+            A = capi.DeviceArray(ct.buf, np.int64, (d, n // d, d, 2, l), (0, d * l, l, n * l, 1), ct.offset)
+            B = capi.DeviceArray(self.arena_buf, np.int64, (d, 1, d, 1, l), (d * l, 0, l, 0, 1), o_diag)
+            perms3 = capi.DeviceArray(perms.buf, np.int64, (d, n // d, d), (n, d, 1), perms.offset)
+            o = capi.DeviceArray(self.arena_buf, np.int64, (n // d, d, 2, l), (d * l, l, n * l, 1),
+                                 o_diag + diag_bytes(l, d))
+            return {"modmul_axis_sum": lambda: capi.call("heal_modmul_axis_sum", A, B, p, perms3, 1, o, 0)}
+        R = self._view(off, (d, 2, n, l))
+        R5 = self._view(off, (d, 2, n // d, d, l))
+        diag = self._view(o_diag, (d, 1, 1, d, l))
+        src = ct.reshape((1, 2, n, l)).expand(0, d)
+        return {"permute": lambda: capi.call("heal_permute", src, perms, R, 0, 2),
+                "modmul": lambda: capi.call("heal_modmul_ttt", R5, diag, p, R5),
+                "axis_modsum": lambda: capi.call("heal_axis_modsum", R, p, out, 0)}
+
     def enqueue(self, req: Request, off: int, stream):
-        """Issues the request's copies and three HEAL calls on `stream`; the
-        output lands in a pinned host array returned with the event."""
+        """Issues the request's copies and HEAL calls on `stream`; the output
+        lands in a pinned host array returned with the event."""
         capi, n, l, d = self.capi, req.n, req.l, req.d
         capi.check(capi.lib().heal_set_stream(stream.cuda_stream))
         try:
-            first = full_diag_bytes(n, l, d) if self.fused else stack_bytes(n, l, d)
-            o_stack, o_diag = off, off + first
-            o_out = o_diag + diag_bytes(l, d)
-            R = self._view(o_stack, (d, 2, n, l))
-            diag = self._view(o_diag, (d, 1, 1, d, l))
-            out = self._view(o_out, (2, n, l))
+            o_diag = off if self.fused else off + stack_bytes(n, l, d)
+            out = self._view(o_diag + diag_bytes(l, d), (2, n, l))
             host = self.host_mats[(d, l, req.mat)][n]
-            capi.check(capi.lib().heal_h2d_async(ctypes.c_void_p(diag.ptr), ctypes.c_void_p(host.data_ptr()),
-                                                 diag_bytes(l, d)))
-            ct = self.ct[(n, l)][req.ct]
-            src = ct.reshape((1, 2, n, l)).expand(0, d)
-            p = self.p[(n, l)]
-            if self.fused:
-                # the diagonals tiled over the N slots ([d, N, L], one broadcast
-                # copy), then sum_i rot_i(ct) * diag_i in one fused call over
-                # S = [d, N, 2, L]: both polynomials of a slot read one diagonal value
-                full = self._view(o_stack, (d, n // d, d, l))
-                tiled = capi.DeviceArray(self.arena_buf, np.int64, (d, n // d, d, l), (d * l, 0, l, 1), o_diag)
-                capi.call("heal_copy_strided", tiled, full)
-                a = ct.reshape((1, 2, n, l)).moveaxis(1, 2).expand(0, d)
-                b = self._view(o_stack, (d, n, 1, l))
-                capi.call("heal_modmul_axis_sum", a, b, p, self.perms[(n, d)], 1, out.moveaxis(0, 1), 0)
-            else:
-                capi.call("heal_permute", src, self.perms[(n, d)], R, 0, 2)
-                R5 = self._view(o_stack, (d, 2, n // d, d, l))
-                capi.call("heal_modmul_ttt", R5, diag, p, R5)
-                capi.call("heal_axis_modsum", R, p, out, 0)
+            capi.check(capi.lib().heal_h2d_async(ctypes.c_void_p(self.arena_buf.ptr.value + o_diag),
+                                                 ctypes.c_void_p(host.data_ptr()), diag_bytes(l, d)))
+            for fn in self.calls(req, off).values():
+                fn()
             res = self.torch.empty((2, n, l), dtype=self.torch.int64, pin_memory=True)
             capi.check(capi.lib().heal_d2h_async(ctypes.c_void_p(res.data_ptr()), ctypes.c_void_p(out.ptr),
                                                  out_bytes(n, l)))
@@ -293,36 +298,14 @@ class MatVecServer:
     def split_ms(self, req: Request, reps: int = 5) -> dict:
         """Median CUDA-event time of each HEAL call of the request (its
         copies excluded), for the server's path."""
-        capi, torch, n, l, d = self.capi, self.torch, req.n, req.l, req.d
+        torch = self.torch
         req.fused = self.fused
         off = self.arena.alloc(req.footprint())
         stream = self.streams[0]
-        capi.check(capi.lib().heal_set_stream(stream.cuda_stream))
+        self.capi.check(self.capi.lib().heal_set_stream(stream.cuda_stream))
         try:
-            first = full_diag_bytes(n, l, d) if self.fused else stack_bytes(n, l, d)
-            o_diag = off + first
-            out = self._view(o_diag + diag_bytes(l, d), (2, n, l))
-            ct = self.ct[(n, l)][req.ct]
-            p = self.p[(n, l)]
-            if self.fused:
-                full = self._view(off, (d, n // d, d, l))
-                tiled = capi.DeviceArray(self.arena_buf, np.int64, (d, n // d, d, l), (d * l, 0, l, 1), o_diag)
-                a = ct.reshape((1, 2, n, l)).moveaxis(1, 2).expand(0, d)
-                b = self._view(off, (d, n, 1, l))
-                o = out.moveaxis(0, 1)
-                calls = {"tile_diagonals": lambda: capi.call("heal_copy_strided", tiled, full),
-                         "modmul_axis_sum": lambda: capi.call("heal_modmul_axis_sum", a, b, p, self.perms[(n, d)],
-                                                              1, o, 0)}
-            else:
-                R = self._view(off, (d, 2, n, l))
-                R5 = self._view(off, (d, 2, n // d, d, l))
-                diag = self._view(o_diag, (d, 1, 1, d, l))
-                src = ct.reshape((1, 2, n, l)).expand(0, d)
-                calls = {"permute": lambda: capi.call("heal_permute", src, self.perms[(n, d)], R, 0, 2),
-                         "modmul": lambda: capi.call("heal_modmul_ttt", R5, diag, p, R5),
-                         "axis_modsum": lambda: capi.call("heal_axis_modsum", R, p, out, 0)}
             res = {}
-            for name, fn in calls.items():
+            for name, fn in self.calls(req, off).items():
                 ts = []
                 for _ in range(reps):
                     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -334,7 +317,7 @@ class MatVecServer:
                 res[name] = sorted(ts)[len(ts) // 2]
             return res
         finally:
-            capi.check(capi.lib().heal_set_stream(None))
+            self.capi.check(self.capi.lib().heal_set_stream(None))
             self.arena.free(off)
 
     def alone(self, req: Request) -> np.ndarray:
@@ -372,13 +355,11 @@ class MatVecServer:
         """Algorithmic bytes of one request, copies to and from the host
         included.  Three calls: permute writes the stack (the ciphertext is
         read once per rotation, from L2), modmul reads it and writes it,
-        axis_modsum reads it and writes the output.  Fused: the tiling copy
-        writes the full diagonals, modmul_axis_sum reads them once and the
-        ciphertext once and writes the output."""
+        axis_modsum reads it and writes the output.  Fused: the rotation
+        table (d x N indices), the ciphertext and the diagonals are read once
+        and the output written once."""
         n, l, d = req.n, req.l, req.d
         io = 2 * diag_bytes(l, d) + 2 * out_bytes(n, l)   # H2D + its read, D2H + its write
         if req.fused:
-            f = full_diag_bytes(n, l, d)
-            return 2 * f + out_bytes(n, l) + io
-        s = stack_bytes(n, l, d)
-        return 4 * s + io
+            return d * n * 8 + out_bytes(n, l) + out_bytes(n, l) + io
+        return 4 * stack_bytes(n, l, d) + io

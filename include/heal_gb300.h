@@ -258,9 +258,12 @@ int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tens
  * `axis` re-inserted; axis in [0, ndim(S) - 2]; p of shape [S[-1]]), and
  * a' = a when perms is NULL, else a gathered like permute with
  * elementwise_axis = axis: a'[c] = a[c with c[perm_axis] <- perms[c[axis],
- * c[perm_axis]]], perms of shape [S[axis], S[perm_axis]].  Bit-identical to
- * the separate calls; the product is never written.  Errors as axis_modsum /
- * permute. */
+ * c[perm_axis]]], perms of shape [S[axis], S[perm_axis]].  Perms of shape
+ * [S[axis], S[perm_axis], S[perm_axis + 1]] (linear across its last two
+ * axes) gather over the two axes taken as one flattened axis, a linear
+ * across them: permute of a with those axes reshaped into one.
+ * Bit-identical to the separate calls; the product is never written.
+ * Errors as axis_modsum / permute. */
 int heal_modmul_axis_sum(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
                          int64_t perm_axis, const heal_tensor *result, int64_t axis);
 

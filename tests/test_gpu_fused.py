@@ -70,6 +70,20 @@ def test_matches_composition_non_canonical(dt):
         assert np.array_equal(fused(a, b, p, axis), composed(a, b, p, axis)), axis
 
 
+@pytest.mark.parametrize("bits", [40, 61, 62, 63])
+def test_non_negative_terms_above_q(bits):
+    """Terms in [q, 2^bitlen(q)) (non-canonical, non-negative) and terms
+    above that, against the composition."""
+    rng = np.random.default_rng(bits)
+    p = np.array([(1 << (bits - 1)) + 12345, (1 << (bits - 1)) + 3], np.int64)
+    lo, hi = int(p.min()), (1 << bits) - 1
+    a = rng.integers(lo, hi, size=(37, 6, 2), dtype=np.int64)
+    b = rng.integers(lo, hi, size=(37, 6, 2), dtype=np.int64)
+    assert np.array_equal(fused(a, b, p, 0), composed(a, b, p, 0))
+    b[5, 3, 1] = np.int64((1 << 62) + 5)                       # one term far above
+    assert np.array_equal(fused(a, b, p, 0), composed(a, b, p, 0))
+
+
 def test_rotation_sum_matches_permute_modmul_axis_modsum():
     rng = np.random.default_rng(3)
     d, n, l = 8, 256, 3
@@ -85,6 +99,37 @@ def test_rotation_sum_matches_permute_modmul_axis_modsum():
     a2 = np.broadcast_to(np.moveaxis(ct, 0, 1)[None], (d, n, 2, l))
     got = fused(a2, diag.reshape(d, n, 1, l), p, 0, perms, 1)
     assert np.array_equal(np.moveaxis(got, 1, 0), want)
+
+
+def test_rotation_sum_over_flattened_slot_pair():
+    """The serving layout: S = [d, N/d, d, 2, L], slot j = u * d + s; the
+    diagonals enter as [d, 1, d, 1, L] and the rotation gathers over (u, s)."""
+    d, n, l = 8, 256, 3
+    qs = P.ntt_primes(1 << 40, n, l)
+    p = np.array(qs, np.int64)
+    ct = P.residues(6, (2, n, l), qs)
+    perms = np.stack([P.galois_perm(n, pow(5, i, 2 * n)) for i in range(d)]).astype(np.int64)
+    diag = P.residues(7, (d, d, l), qs)                       # diag[i, s, t]
+    tiled = np.broadcast_to(diag[:, None, :, :], (d, n // d, d, l)).reshape(d, 1, n, l)
+    want = composed(np.broadcast_to(ct[None], (d, 2, n, l)), tiled, p, 0, perms, 2)   # [2, n, l]
+    dct, dperm = up(ct), up(perms)
+    A = capi.DeviceArray(dct.buf, np.int64, (d, n // d, d, 2, l), (0, d * l, l, n * l, 1))
+    B = capi.DeviceArray(up(diag).buf, np.int64, (d, 1, d, 1, l), (d * l, 0, l, 0, 1))
+    P3 = capi.DeviceArray(dperm.buf, np.int64, (d, n // d, d), (n, d, 1))
+    out = capi.DeviceArray.empty((2, n, l), np.int64)
+    O4 = capi.DeviceArray(out.buf, np.int64, (n // d, d, 2, l), (d * l, l, n * l, 1))
+    capi.call("heal_modmul_axis_sum", A, B, up(p), P3, 1, O4, 0)
+    assert np.array_equal(out.numpy(), want)
+    # a gather pair that a does not walk linearly, perms that are not linear, the reduced axis inside the pair
+    A_bad = capi.DeviceArray(dct.buf, np.int64, (d, n // d, d, 2, l), (0, l, l, n * l, 1))
+    P3_bad = capi.DeviceArray(up(np.zeros((d, n // d, 2 * d), np.int64)).buf, np.int64, (d, n // d, d),
+                              (n * 2, 2 * d, 1))
+    for args in ((A_bad, B, up(p), P3, 1, O4, 0), (A, B, up(p), P3_bad, 1, O4, 0)):
+        with pytest.raises(ValueError):
+            capi.call("heal_modmul_axis_sum", *args)
+    with pytest.raises(ValueError):
+        capi.call("heal_modmul_axis_sum", A, B, up(p), capi.DeviceArray(dperm.buf, np.int64, (n // d, d, 2),
+                                                                         (d, 1, 0)), 0, O4, 1)
 
 
 def test_argument_errors():
