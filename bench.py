@@ -12,8 +12,10 @@ Printed: one JSON line (rank 0).  `value` is chains/s with inputs resident
 in HBM, timed with CUDA events on the library stream; inputs rotate through
 8 ciphertexts (192 MiB) and 8 outputs, more than the 126 MiB L2, so no step
 reads the previous step's data from L2.  `e2e` is the same through the C ABI
-from pinned host buffers (H2D of ct and D2H of the result inside the timed
-region).  `roofline` covers the batched NTT of the digits.  `cpu_baseline`
+from pinned host buffers (H2D of ct and D2H of the result of every step
+inside the timed region, on their own streams so that they overlap the
+chains of neighbouring steps; `e2e.serial_value` is the same back to back).
+`roofline` covers the batched NTT of the digits.  `cpu_baseline`
 times the CPU oracle (a restatement of HEAL's example_impl) on this host.
 
 --impl reference times the CPU oracle itself on all host cores, four limbs of
@@ -279,29 +281,79 @@ def our_arm(args):
     split_ms = {n: statistics.median(evs[s][ci].elapsed_time(evs[s][ci + 1]) for s in range(args.steps))
                 for ci, n in enumerate(names)}
 
-    # ---- end to end through the C ABI from pinned host memory
+    # ---- end to end through the C ABI from pinned host memory.  Every step
+    # copies its ciphertext in (H2D) and its result out (D2H) inside the timed
+    # region; the copies run on their own streams, double-buffered, so the
+    # H2D of step s+1 and the D2H of step s-1 overlap the chain of step s.
     nbytes = 2 * N * L * 8
     import ctypes
-    pin_in, pin_out = ctypes.c_void_p(), ctypes.c_void_p()
-    capi.check(capi.lib().heal_host_alloc(nbytes, ctypes.byref(pin_in)))
-    capi.check(capi.lib().heal_host_alloc(nbytes, ctypes.byref(pin_out)))
+    lib = capi.lib()
+    pin_in = ctypes.c_void_p()
+    capi.check(lib.heal_host_alloc(nbytes, ctypes.byref(pin_in)))
+    pin_out = [ctypes.c_void_p() for _ in range(2)]
+    for p_ in pin_out:
+        capi.check(lib.heal_host_alloc(nbytes, ctypes.byref(p_)))
     ctypes.memmove(pin_in, cts_host[0].ctypes.data, nbytes)
-    dev_in, dev_out = cts[0], outs[0]
+    dev_in = [capi.DeviceArray.empty(ch.shape(), np.int64, zero=False) for _ in range(2)]
+    dev_out = [capi.DeviceArray.empty(ch.shape(), np.int64, zero=False) for _ in range(2)]
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    ev_in, ev_comp, ev_out = ([torch.cuda.Event() for _ in range(2)] for _ in range(3))
+    use = lambda st: capi.check(lib.heal_set_stream(st.cuda_stream if st is not None else None))
 
     def e2e_step(s):
-        capi.check(capi.lib().heal_h2d_async(ctypes.c_void_p(dev_in.ptr), pin_in, nbytes))
-        ch.run(dev_in, dev_out)
-        capi.check(capi.lib().heal_d2h_async(pin_out, ctypes.c_void_p(dev_out.ptr), nbytes))
+        b = s % 2
+        s_in.wait_event(ev_comp[b])                       # the chain that last read dev_in[b]
+        use(s_in)
+        capi.check(lib.heal_h2d_async(ctypes.c_void_p(dev_in[b].ptr), pin_in, nbytes))
+        ev_in[b].record(s_in)
+        stream.wait_event(ev_in[b])
+        stream.wait_event(ev_out[b])                      # the copy that last read dev_out[b]
+        use(None)
+        ch.run(dev_in[b], dev_out[b])
+        ev_comp[b].record(stream)
+        s_out.wait_event(ev_comp[b])
+        use(s_out)
+        capi.check(lib.heal_d2h_async(pin_out[b], ctypes.c_void_p(dev_out[b].ptr), nbytes))
+        ev_out[b].record(s_out)
+        use(None)
+
+    def e2e_timed(steps):
+        barrier()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        s_in.wait_event(start)
+        for s in range(steps):
+            e2e_step(s)
+        stream.wait_event(ev_out[(steps - 1) % 2])
+        stream.wait_event(ev_out[steps % 2])
+        stop.record(stream)
+        stop.synchronize()
+        barrier()
+        return max_over_ranks(start.elapsed_time(stop), world, "cuda")
 
     for w in range(args.warmup):
         e2e_step(w)
-    e2e_ms, _ = timed(e2e_step, args.steps)
+    e2e_ms = e2e_timed(args.steps)
     e2e = whole_job_rate(args.steps, world, e2e_ms)
-    got = np.frombuffer((ctypes.c_char * nbytes).from_address(pin_out.value), dtype=np.int64).reshape(ch.shape())
+    torch.cuda.synchronize()
     want = outs[0].numpy()
-    assert np.array_equal(got, want), "e2e output differs from the resident run"
+    for p_ in pin_out:
+        got = np.frombuffer((ctypes.c_char * nbytes).from_address(p_.value), dtype=np.int64).reshape(ch.shape())
+        assert np.array_equal(got, want), "e2e output differs from the resident run"
+
+    # the same without overlap: H2D, chain, D2H back to back on one stream
+    def serial_step(s):
+        capi.check(lib.heal_h2d_async(ctypes.c_void_p(dev_in[0].ptr), pin_in, nbytes))
+        ch.run(dev_in[0], dev_out[0])
+        capi.check(lib.heal_d2h_async(pin_out[0], ctypes.c_void_p(dev_out[0].ptr), nbytes))
+
+    for w in range(args.warmup):
+        serial_step(w)
+    serial_ms, _ = timed(serial_step, args.steps)
+    e2e_serial = whole_job_rate(args.steps, world, serial_ms)
     capi.lib().heal_host_free(pin_in)
-    capi.lib().heal_host_free(pin_out)
+    for p_ in pin_out:
+        capi.lib().heal_host_free(p_)
 
     # ---- the other configurations (reported beside the headline)
     configs = {}
@@ -328,7 +380,9 @@ def our_arm(args):
                              "frac": achieved / hbm, "algorithmic_bytes": ntt_bytes,
                              "ms_per_call": ntt_call_ms,
                              "traffic": traffic.get("bytes_per_call") if traffic else None},
-                "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+                "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                        "pipeline": "H2D, chain and D2H of consecutive steps overlapped on three streams",
+                        "serial_value": e2e_serial},
                 "gpu_launches": launches, "launches_per_step": launches / args.steps,
                 "split_ms": split_ms,
                 "clocks": clocks, "cpu_baseline": cpu, "configs": configs}
