@@ -394,6 +394,16 @@ void permute(const std::shared_ptr<DeviceTensor<T>> &a, const std::shared_ptr<De
   check(heal_permute(&A, &PM, &R, elementwise_axis, perm_axis));
 }
 
+template <typename T>
+void modmul_axis_sum(const std::shared_ptr<DeviceTensor<T>> &a, const std::shared_ptr<DeviceTensor<T>> &b,
+                     const std::shared_ptr<DeviceTensor<T>> &p, const std::shared_ptr<DeviceTensor<T>> &perms,
+                     int64_t perm_axis, std::shared_ptr<DeviceTensor<T>> &result, int64_t axis) {
+  heal_tensor A = need(a, "a"), B = need(b, "b"), P = need(p, "p"), R = need(result, "result");
+  heal_tensor PM;
+  if (perms) PM = perms->desc();
+  check(heal_modmul_axis_sum(&A, &B, &P, perms ? &PM : nullptr, perm_axis, &R, axis));
+}
+
 void synchronize() { check(heal_synchronize()); }
 
 // ============================================================ instantiations
@@ -431,6 +441,9 @@ void synchronize() { check(heal_synchronize()); }
   template void modneg_tt<T>(const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &,  \
                              std::shared_ptr<DeviceTensor<T>> &);                                                \
   template void modneg_tc<T>(const std::shared_ptr<DeviceTensor<T>> &, T, std::shared_ptr<DeviceTensor<T>> &);    \
+  template void modmul_axis_sum<T>(const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
+                                   const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
+                                   int64_t, std::shared_ptr<DeviceTensor<T>> &, int64_t);                           \
   template void axis_modsum<T>(const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
                                std::shared_ptr<DeviceTensor<T>> &, int64_t);                                    \
   template void g_decomposition<T>(const std::shared_ptr<DeviceTensor<T>> &, std::shared_ptr<DeviceTensor<T>> &,  \

@@ -120,6 +120,13 @@ template <typename T>
 void modneg_tc(const std::shared_ptr<DeviceTensor<T>> &a, T p_scalar, std::shared_ptr<DeviceTensor<T>> &result);
 template <typename T>
 std::shared_ptr<DeviceTensor<T>> moveaxis(const std::shared_ptr<DeviceTensor<T>> &tensor, int64_t src, int64_t dst);
+// result = axis_modsum(modmul(a', b, p), axis), a' = a gathered by perms (may
+// be null) along perm_axis: DeviceDispatcher.modmul_axis_sum
+// (device_interface.py:67-68); see heal_modmul_axis_sum.
+template <typename T>
+void modmul_axis_sum(const std::shared_ptr<DeviceTensor<T>> &a, const std::shared_ptr<DeviceTensor<T>> &b,
+                     const std::shared_ptr<DeviceTensor<T>> &p, const std::shared_ptr<DeviceTensor<T>> &perms,
+                     int64_t perm_axis, std::shared_ptr<DeviceTensor<T>> &result, int64_t axis);
 template <typename T>
 std::shared_ptr<DeviceTensor<T>> get_slice(const std::shared_ptr<DeviceTensor<T>> &tensor, int64_t axis,
                                            int64_t start, int64_t stop, int64_t step);

@@ -3,8 +3,8 @@
 // Same module name, class names and function names as HEAL's
 // example_impl/py_bindings.cpp:87-133 (DeviceTensor{32,64,float64};
 // <op>_{32,64,float64}), so python_execution/lattica_heal_runtime/py_wrapper.py
-// imports it unchanged.  Added: mod_*, modneg_*, moveaxis_*, get_slice_* and
-// synchronize(), which HEAL's module does not export.
+// imports it unchanged.  Added: mod_*, modneg_*, moveaxis_*, get_slice_*, view_*,
+// modmul_axis_sum_* and synchronize(), which HEAL's module does not export.
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
 #include <torch/extension.h>
@@ -34,6 +34,11 @@ static void bind_tensor(py::module_ &m, const std::string &sfx) {
   m.def(("moveaxis_" + sfx).c_str(), &moveaxis<T>, py::arg("tensor"), py::arg("source"), py::arg("destination"));
   m.def(("get_slice_" + sfx).c_str(), &get_slice<T>, py::arg("tensor"), py::arg("axis"), py::arg("start"),
         py::arg("stop"), py::arg("step") = 1);
+  // a new view object of the same buffer, dims and strides
+  m.def(("view_" + sfx).c_str(), [](const std::shared_ptr<D> &t) {
+    if (!t) throw std::invalid_argument("tensor pointer must not be null.");
+    return std::make_shared<D>(*t);
+  }, py::arg("tensor"));
 }
 
 template <typename T>
@@ -57,6 +62,8 @@ static void bind_compute(py::module_ &m, const std::string &sfx) {
   m.def(("ntt_" + sfx).c_str(), &ntt<T>);
   m.def(("intt_" + sfx).c_str(), &intt<T>);
   m.def(("permute_" + sfx).c_str(), &permute<T>);
+  m.def(("modmul_axis_sum_" + sfx).c_str(), &modmul_axis_sum<T>, py::arg("a"), py::arg("b"), py::arg("p"),
+        py::arg("perms"), py::arg("perm_axis"), py::arg("result"), py::arg("axis"));
 }
 
 PYBIND11_MODULE(lattica_hw, m) {
