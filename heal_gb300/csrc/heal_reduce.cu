@@ -90,24 +90,28 @@ __global__ void __launch_bounds__(256) axis_modsum_kernel(const __grid_constant_
       R[orr] = 0;
       continue;
     }
-    // the reference's running sum, in order; loads go out kBatch at a time
-    constexpr int kBatch = 8;
+    // the reference's running sum, in order; on long axes the loads go out
+    // kBatch at a time (full batches, then the remainder one by one)
+    constexpr int kBatch = 4;
     int64_t sum = 0;
-    for (int64_t k0 = 0; k0 < g.ax_len; k0 += kBatch) {
+    auto step = [&](int64_t v) {
+      if (sum >= 0 && v >= 0 && q > 0) {
+        uint64_t x = (uint64_t)sum + (uint64_t)v;
+        sum = v < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
+      } else {
+        sum = crem128((i128)sum + (i128)v, q);
+      }
+    };
+    const T *pa = A + oa;
+    int64_t k = 0;
+    for (; k + kBatch <= g.ax_len; k += kBatch) {
       int64_t v[kBatch];
 #pragma unroll
-      for (int j = 0; j < kBatch; ++j) v[j] = k0 + j < g.ax_len ? (int64_t)A[oa + (k0 + j) * g.ax_stride] : 0;
+      for (int j = 0; j < kBatch; ++j) v[j] = (int64_t)pa[(k + j) * g.ax_stride];
 #pragma unroll
-      for (int j = 0; j < kBatch; ++j) {
-        if (k0 + j >= g.ax_len) break;
-        if (sum >= 0 && v[j] >= 0 && q > 0) {
-          uint64_t x = (uint64_t)sum + (uint64_t)v[j];
-          sum = v[j] < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
-        } else {
-          sum = crem128((i128)sum + (i128)v[j], q);
-        }
-      }
+      for (int j = 0; j < kBatch; ++j) step(v[j]);
     }
+    for (; k < g.ax_len; ++k) step((int64_t)pa[k * g.ax_stride]);
     R[orr] = (T)sum;
   }
 }
