@@ -237,7 +237,8 @@ def our_arm(args):
         ms = max_over_ranks(start.elapsed_time(stop), world, "cuda")
         return ms, capi.launches() - l0
 
-    # ---- correctness of the timed configuration (one step, spot-checked)
+    # ---- NTT plans for the chain's shapes (the autotuner, before any timing)
+    plans = ch.tune(cts[0]) if not args.no_tune else None
     ch.run(cts[0], outs[0])
     chain_step = lambda s: ch.run(cts[s % RING], outs[s % RING])
     for w in range(args.warmup):
@@ -384,7 +385,7 @@ def our_arm(args):
                         "pipeline": "H2D, chain and D2H of consecutive steps overlapped on three streams",
                         "serial_value": e2e_serial},
                 "gpu_launches": launches, "launches_per_step": launches / args.steps,
-                "split_ms": split_ms,
+                "split_ms": split_ms, "ntt_plans": plans,
                 "clocks": clocks, "cpu_baseline": cpu, "configs": configs}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -622,6 +623,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-configs", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="default NTT plans instead of autotuned ones")
     ap.add_argument("--configs", default="cfg1,cfg3,cfg4,cfg5",
                     help="comma-separated configurations reported beside the headline")
     ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request"])

@@ -50,6 +50,18 @@ class KeyswitchChain:
     def shape(self):
         return (2, self.n, 1, self.L)
 
+    def tune(self, ct: capi.DeviceArray, reps: int = 5) -> dict:
+        """Runs the NTT autotuner on the chain's two transform shapes (the
+        INTT of the ciphertext, the NTT of the digits) and keeps the fastest
+        plans for every later call; returns them.  Overwrites the chain's
+        intermediate tensors only."""
+        d = self.dev
+        inv = capi.autotune_ntt(True, ct, d["p"], d["perm"], d["itw"], d["minv"], self.x, reps)
+        capi.call("heal_g_decomposition", self.x, self.dig, self.D, self.bits)
+        fwd = capi.autotune_ntt(False, self.dig_flat, d["p_t"], d["perm"], d["tw_t"], None, self.dn, reps)
+        return {"intt": {"tile_limbs": inv[0], "first_pass_log2": inv[1]},
+                "ntt": {"tile_limbs": fwd[0], "first_pass_log2": fwd[1]}}
+
     def run(self, ct: capi.DeviceArray, out: capi.DeviceArray):
         """Enqueues one chain step (6 HEAL calls) on the library stream."""
         d = self.dev

@@ -220,6 +220,12 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
     x.kind = kind;
     x.nsets = m >> pbits;
     x.ngroups_t = (k + c - 1) / c;
+    x.fast_bid = x.ngroups_t < (int64_t)UINT32_MAX && l * r < (int64_t)UINT32_MAX && r < (int64_t)UINT32_MAX;
+    if (x.fast_bid) {
+      x.fd_groups = fastdiv_make((uint32_t)x.ngroups_t);
+      x.fd_nij = fastdiv_make((uint32_t)(l * r));
+      x.fd_r = fastdiv_make((uint32_t)r);
+    }
     return x.nsets * l * r * x.ngroups_t;
   };
 

@@ -45,6 +45,8 @@ struct NttArgs {
   int kind;
   int64_t nsets;      // sets (strided) or blocks per column
   int64_t ngroups_t;  // ceil(k / C)
+  int fast_bid;       // ngroups_t, l * r and r below 2^32: 32-bit block-index split
+  FastDiv fd_groups, fd_nij, fd_r;
   const int32_t *load_map;
   const int32_t *store_gather;
   const int32_t *store_scatter;
@@ -130,14 +132,27 @@ __device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
   // segments of one set are read back to back (one DRAM line serves them
   // all), and the CTAs that share twiddle rows (same set and limbs, other
   // i, j) run within a window of ngroups_t * l * r blocks.
-  const int64_t bid = blockIdx.x;
-  const int64_t nij = g.l * g.r;
-  const int64_t tg = bid % g.ngroups_t;
-  const int64_t rest = bid / g.ngroups_t;
-  const int64_t ij = rest % nij;
-  x.rset = rest / nij;
-  x.j = ij % g.r;
-  x.i = ij / g.r;
+  int64_t tg;
+  if (g.fast_bid) {  // blockIdx.x < 2^31: divisions by invariant 32-bit divisors
+    const uint32_t bid = blockIdx.x;
+    const uint32_t rest = fastdiv(bid, g.fd_groups);
+    tg = bid - rest * g.fd_groups.d;
+    const uint32_t rs = fastdiv(rest, g.fd_nij);
+    const uint32_t ij = rest - rs * g.fd_nij.d;
+    x.rset = rs;
+    const uint32_t ii = fastdiv(ij, g.fd_r);
+    x.i = ii;
+    x.j = ij - ii * g.fd_r.d;
+  } else {
+    const int64_t bid = blockIdx.x;
+    const int64_t nij = g.l * g.r;
+    tg = bid % g.ngroups_t;
+    const int64_t rest = bid / g.ngroups_t;
+    const int64_t ij = rest % nij;
+    x.rset = rest / nij;
+    x.j = ij % g.r;
+    x.i = ij / g.r;
+  }
   x.t0 = tg * g.C;
   x.G = g.kind == KIND_BLOCK ? g.nsets + x.rset : 1;
   return x;

@@ -12,6 +12,8 @@ static int launch_with_smem(Kern kern, const NttArgs &a, int64_t nblocks, int th
     HEAL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     attr_set = true;
   }
+  if (nblocks < 1 || nblocks > 0x7FFFFFFF)  // one CTA per tile along grid x; the tile index is 31-bit
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT: more than 2^31 - 1 tiles in one call");
   kern<<<(unsigned)nblocks, threads, smem, stream()>>>(a);
   return check_launch("ntt_pass");
 }
