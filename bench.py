@@ -574,8 +574,9 @@ def ntt_probe(args):
     """--mode ntt: one batched NTT alone, for ncu captures of the pass
     kernels.  --probe digits: [batch, 65536, 1, 72] int64 under the chain's
     50-bit primes tiled 3x (the digit tensor of batch/2 chains); --probe cfg4:
-    [batch, 65536, 1, 32] int32 under 31-bit primes.  Prints one JSON line
-    with the CUDA-event time per call."""
+    [batch, 65536, 1, 32] int32 under 31-bit primes; --probe ct-intt: the INTT
+    of [batch, 65536, 1, 24] int64 (the chain's ciphertext).  Prints one JSON
+    line with the CUDA-event time per call."""
     import torch
     import heal_gb300
     from heal_gb300 import capi
@@ -583,9 +584,14 @@ def ntt_probe(args):
     heal_gb300.build()
     capi.check(capi.lib().heal_init(0))
     stream = torch.cuda.ExternalStream(capi.stream())
+    inverse = args.probe == "ct-intt"
     if args.probe == "cfg4":
         dt, k, qs = np.int32, 32, P.ntt_primes(1 << 31, N, 32)
         p_t, perm, tw_t, itw, minv = P.ntt_tables(qs, N, dt)
+    elif inverse:
+        dt, k = np.int64, L
+        qs = P.ntt_primes(1 << BOUND, N, L)
+        p_t, perm, tw_t, itw, minv = P.ntt_tables(qs, N)
     else:
         dt, k = np.int64, L * D
         qs = P.ntt_primes(1 << BOUND, N, L)
@@ -594,8 +600,11 @@ def ntt_probe(args):
     shape = (args.batch, N, 1, k)
     x = capi.DeviceArray.from_numpy(P.residues(3, shape, p_t, dt))
     y = capi.DeviceArray.empty(shape, dt)
-    dev = [capi.DeviceArray.from_numpy(v) for v in (p_t, perm, tw_t)]
-    call = lambda: capi.call("heal_ntt", x, dev[0], dev[1], dev[2], None, None, y)
+    dev = [capi.DeviceArray.from_numpy(v) for v in (p_t, perm, itw if inverse else tw_t, minv)]
+    if inverse:
+        call = lambda: capi.call("heal_intt", x, dev[0], dev[1], dev[2], dev[3], None, None, y)
+    else:
+        call = lambda: capi.call("heal_ntt", x, dev[0], dev[1], dev[2], None, None, y)
     for _ in range(args.warmup):
         call()
     capi.synchronize()
@@ -631,7 +640,7 @@ def main():
     ap.add_argument("--n", type=int, default=1 << 14, help="--mode request: ring degree")
     ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
     ap.add_argument("--batch", type=int, default=4)
-    ap.add_argument("--probe", default="digits", choices=["digits", "cfg4"])
+    ap.add_argument("--probe", default="digits", choices=["digits", "cfg4", "ct-intt"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

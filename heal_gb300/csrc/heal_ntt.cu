@@ -211,9 +211,9 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   void *tmp = nullptr, *tmp2 = nullptr;
 
   auto cfg = [&](NttArgs &x, int pbits, int kind) -> int64_t {
-    // at most 512 threads per CTA: P * C / kPT <= 512
+    // at most 512 threads per CTA: P * C / (points per thread) <= 512
     int c = C;
-    while (c > 1 && ((int64_t)1 << pbits) * c > 512 * kPT) c /= 2;
+    while (c > 1 && ((int64_t)1 << pbits) * c > ((int64_t)512 << lpt_of(mode, inv))) c /= 2;
     x.p = pbits;
     x.C = c;
     x.logC = ilog2(c);

@@ -5,10 +5,11 @@
 // heal_ntt.cu for how the stages split into passes and why the twiddle of
 // every butterfly equals the reference's).
 //
-// Register-blocked form (P >= 16): each thread keeps 16 points of one
-// column in registers and runs up to 4 stages per step on them (a radix-16
-// group: every twiddle is loaded once per group of butterflies that share
-// it); between steps the points are exchanged through a shared-memory tile.
+// Register-blocked form: each thread keeps 8 points (16 in the forward
+// canonical 32-bit mode) of one column in registers and runs up to 3 (4)
+// stages per step on them (a radix-8 / radix-16 group: every twiddle is loaded
+// once per group of butterflies that share it); between steps the points are
+// exchanged through a shared-memory tile.
 // The tile index of point s is XOR-swizzled, s ^ ((s >> 4) & 15), so that
 // both the strided (s = r + 16j) and the blocked (s = 16r + j) access
 // patterns of a step hit distinct banks.
@@ -25,13 +26,6 @@ namespace heal {
 
 enum { KIND_STRIDED = 0, KIND_BLOCK = 1 };
 
-// log2 of the points one thread of the register kernel holds (a radix-2^kLPT
-// step per shared-memory exchange)
-#ifndef HEAL_NTT_LPT
-#define HEAL_NTT_LPT 3
-#endif
-constexpr int kLPT = HEAL_NTT_LPT;
-constexpr int kPT = 1 << kLPT;
 
 struct NttArgs {
   const void *src;
@@ -86,6 +80,21 @@ struct Word<false> {
 // [0, 2q) with one conditional subtraction per butterfly instead of three;
 // every pass still ends on canonical residues.
 enum { MODE_N32 = 0, MODE_N32_LAZY = 1, MODE_W64_LAZY = 2 };
+
+// log2 of the points one thread of the register kernel holds (a radix-2^lpt
+// step per shared-memory exchange): 16 points for the forward transform in
+// canonical 32-bit words, 8 otherwise (measured best for each: the 64-bit
+// modes need two registers per point, and the inverse and lazy 32-bit
+// kernels ran slower with 16)
+#ifndef HEAL_NTT_LPT
+#define HEAL_NTT_LPT 3
+#endif
+#ifndef HEAL_NTT_LPT_N32_FWD
+#define HEAL_NTT_LPT_N32_FWD 4
+#endif
+__host__ __device__ constexpr int lpt_of(int mode, bool inv) {
+  return (mode == MODE_N32 && !inv) ? HEAL_NTT_LPT_N32_FWD : HEAL_NTT_LPT;
+}
 
 // y * w mod q up to one extra q: [0, 2q) for any y (Shoup, no final step)
 template <bool WIDE>
@@ -332,7 +341,7 @@ __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ 
 // --------------------------------------------------- register-blocked
 // Point held in register e (0 .. kPT-1) by thread r during step `step`
 // (steps of kLPT stages; the last one may be shorter).
-template <bool INV, int LOGP>
+template <bool INV, int LOGP, int kLPT>
 __device__ __forceinline__ int point_of(int step, int r, int e) {
   const int st0 = kLPT * step;
   const int q = (LOGP - st0) < kLPT ? (LOGP - st0) : kLPT;
@@ -350,11 +359,12 @@ __device__ __forceinline__ int point_of(int step, int r, int e) {
 // One register step: stages [kLPT*STEP, kLPT*STEP + qn) on the kPT >> qn
 // sets of 2^qn points this thread holds.
 template <int MODE, bool INV, int LOGP, int STEP>
-__device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W (&v)[kPT], int r, int64_t G,
+__device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W (&v)[1 << lpt_of(MODE, INV)], int r, int64_t G,
                                          const typename Word<MODE == MODE_W64_LAZY>::Pair *twp,
                                          typename Word<MODE == MODE_W64_LAZY>::W q) {
   constexpr bool WIDE = MODE == MODE_W64_LAZY;
   constexpr bool LAZY = MODE != MODE_N32;
+  constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
   typedef typename Word<WIDE>::W W;
   typedef typename Word<WIDE>::Pair Pair;
   constexpr int P = 1 << LOGP;
@@ -425,11 +435,12 @@ __device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W
 
 // Steps STEP .. NSTEP-1, exchanging through the shared tile between steps.
 template <int MODE, bool INV, int LOGP, int STEP>
-__device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::W (&v)[kPT], int r, int c, int logC,
+__device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::W (&v)[1 << lpt_of(MODE, INV)], int r, int c, int logC,
                                           int64_t *tile, int64_t G,
                                           const typename Word<MODE == MODE_W64_LAZY>::Pair *twp,
                                           typename Word<MODE == MODE_W64_LAZY>::W q) {
   typedef typename Word<MODE == MODE_W64_LAZY>::W W;
+  constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
   constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
   if constexpr (STEP < NSTEP) {
     if constexpr (STEP > 0) {
@@ -437,10 +448,10 @@ __device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::
       // 32-bit modes); the exact path never shares a CTA with it
       W *wt = reinterpret_cast<W *>(tile);
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) wt[tidx(point_of<INV, LOGP>(STEP - 1, r, e), c, logC)] = v[e];
+      for (int e = 0; e < kPT; ++e) wt[tidx(point_of<INV, LOGP, kLPT>(STEP - 1, r, e), c, logC)] = v[e];
       __syncthreads();
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) v[e] = wt[tidx(point_of<INV, LOGP>(STEP, r, e), c, logC)];
+      for (int e = 0; e < kPT; ++e) v[e] = wt[tidx(point_of<INV, LOGP, kLPT>(STEP, r, e), c, logC)];
       __syncthreads();
     }
     reg_step<MODE, INV, LOGP, STEP>(v, r, G, twp, q);
@@ -452,6 +463,7 @@ template <typename T, int MODE, bool INV, int LOGP>
 __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
   constexpr bool WIDE = MODE == MODE_W64_LAZY;
   constexpr bool LAZY = MODE != MODE_N32;
+  constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
   typedef typename Word<WIDE>::W W;
   typedef typename Word<WIDE>::Pair Pair;
   constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
@@ -475,16 +487,16 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
   if (g.load_map) {
 #pragma unroll
     for (int e = 0; e < kPT; ++e) {
-      raw[e] = act ? load_point<T>(g, x, point_of<INV, LOGP>(0, r, e), t) : 0;
+      raw[e] = act ? load_point<T>(g, x, point_of<INV, LOGP, kLPT>(0, r, e), t) : 0;
       neg |= needs_exact<INV>(g, raw[e], q64);
     }
   } else {
     const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + tq * g.ss[3]) +
-                  x.row_of(g, point_of<INV, LOGP>(0, r, 0)) * g.ss[1];
+                  x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, 0)) * g.ss[1];
     const int64_t rs = rowmul * g.ss[1];
 #pragma unroll
     for (int e = 0; e < kPT; ++e) {
-      raw[e] = act ? (int64_t)p0[point_of<INV, LOGP>(0, 0, e) * rs] : 0;
+      raw[e] = act ? (int64_t)p0[point_of<INV, LOGP, kLPT>(0, 0, e) * rs] : 0;
       neg |= needs_exact<INV>(g, raw[e], q64);
     }
   }
@@ -492,7 +504,7 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
                      (g.scale && g.minv_neg && *g.minv_neg);
   if (exact) {
 #pragma unroll
-    for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP>(0, r, e), c, logC)] = raw[e];
+    for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP, kLPT>(0, r, e), c, logC)] = raw[e];
     __syncthreads();
     exact_tile<T, INV>(g, x, tile);
     return;
@@ -524,12 +536,12 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
     W *wt = reinterpret_cast<W *>(tile);
     if (NSTEP == 1) __syncthreads();  // no exchange ran: the tile may still hold raw loads
 #pragma unroll
-    for (int e = 0; e < kPT; ++e) wt[tidx(point_of<INV, LOGP>(NSTEP - 1, r, e), c, logC)] = v[e];
+    for (int e = 0; e < kPT; ++e) wt[tidx(point_of<INV, LOGP, kLPT>(NSTEP - 1, r, e), c, logC)] = v[e];
     __syncthreads();
     if (act) {
 #pragma unroll
       for (int e = 0; e < kPT; ++e) {
-        const int s = point_of<INV, LOGP>(0, r, e);
+        const int s = point_of<INV, LOGP, kLPT>(0, r, e);
         store_point<T>(g, x, s, t, (int64_t)wt[tidx(g.store_gather[s], c, logC)]);
       }
     }
@@ -543,18 +555,18 @@ __global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ Nt
     for (int e = 0; e < kPT; ++e) {
       W val = v[e];
       if (g.scale) val = mulw<WIDE>(val, mp, q);
-      store_point<T>(g, x, point_of<INV, LOGP>(NSTEP - 1, r, e), t, (int64_t)val);
+      store_point<T>(g, x, point_of<INV, LOGP, kLPT>(NSTEP - 1, r, e), t, (int64_t)val);
     }
     return;
   }
   T *p1 = (T *)g.dst + (x.i * g.ds[0] + x.j * g.ds[2] + t * g.ds[3]) +
-          x.row_of(g, point_of<INV, LOGP>(NSTEP - 1, r, 0)) * g.ds[1];
+          x.row_of(g, point_of<INV, LOGP, kLPT>(NSTEP - 1, r, 0)) * g.ds[1];
   const int64_t rsd = rowmul * g.ds[1];
 #pragma unroll
   for (int e = 0; e < kPT; ++e) {
     W val = v[e];
     if (g.scale) val = mulw<WIDE>(val, mp, q);
-    p1[point_of<INV, LOGP>(NSTEP - 1, 0, e) * rsd] = (T)(int64_t)val;
+    p1[point_of<INV, LOGP, kLPT>(NSTEP - 1, 0, e) * rsd] = (T)(int64_t)val;
   }
 }
 

@@ -21,7 +21,7 @@ static int launch_with_smem(Kern kern, const NttArgs &a, int64_t nblocks, int th
 template <typename T, int MODE, bool INV, int LOGP>
 static int launch_reg(const NttArgs &a, int64_t nblocks) {
   static bool attr = false;
-  const int threads = ((1 << LOGP) / kPT) * a.C;
+  const int threads = ((1 << LOGP) >> lpt_of(MODE, INV)) * a.C;
   const size_t smem = (size_t)(1 << LOGP) * a.C * sizeof(int64_t);
   return launch_with_smem(ntt_reg_kernel<T, MODE, INV, LOGP>, a, nblocks, threads, smem, attr);
 }
@@ -37,7 +37,7 @@ template <typename T, int MODE, bool INV>
 static int launch_typed(const NttArgs &a, int64_t nblocks) {
   switch (a.p) {
     case 3:
-      if constexpr (kLPT <= 3) return launch_reg<T, MODE, INV, 3>(a, nblocks);
+      if constexpr (lpt_of(MODE, INV) <= 3) return launch_reg<T, MODE, INV, 3>(a, nblocks);
       return launch_small<T, MODE == MODE_W64_LAZY, INV>(a, nblocks);
     case 4: return launch_reg<T, MODE, INV, 4>(a, nblocks);
     case 5: return launch_reg<T, MODE, INV, 5>(a, nblocks);
