@@ -116,6 +116,71 @@ __global__ void __launch_bounds__(256) axis_modsum_kernel(const __grid_constant_
   }
 }
 
+// The reference's running sum of one output: sum = (sum + v) % q, C
+// semantics for values outside [0, q).
+__device__ __forceinline__ int64_t running_step(int64_t sum, int64_t v, int64_t q) {
+  if (sum >= 0 && v >= 0 && q > 0) {
+    uint64_t x = (uint64_t)sum + (uint64_t)v;
+    return v < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
+  }
+  return crem128((i128)sum + (i128)v, q);
+}
+
+// Reduced axis innermost in memory: output e of a dense row-major result sums
+// a[e * D + k], k < D (the digit axis of a moved [.., L, D] view).  A thread
+// takes VEC = 16 / sizeof(T) consecutive outputs: their VEC * D inputs are D
+// aligned 16-byte vectors, and the VEC results one 16-byte store.
+struct BlockSumArgs {
+  const void *a, *p;
+  void *out;
+  int64_t nvec;       // outputs / VEC
+  int64_t p_stride;
+  uint32_t last;      // result's last dimension (modulus index = e mod last)
+  FastDiv last_div;
+  Diag *diag;
+};
+
+template <typename T, int D>
+__global__ void __launch_bounds__(256) axis_modsum_blocks_kernel(const __grid_constant__ BlockSumArgs g) {
+  constexpr int VEC = 16 / sizeof(T);
+  const uint4 *A = (const uint4 *)g.a;
+  uint4 *R = (uint4 *)g.out;
+  const T *P = (const T *)g.p;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.nvec;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    union { uint4 w[D]; T x[VEC * D]; } in;
+#pragma unroll
+    for (int k = 0; k < D; ++k) in.w[k] = A[v * D + k];
+    union { uint4 w; T x[VEC]; } out;
+    const uint32_t e0 = (uint32_t)(v * VEC);
+#pragma unroll
+    for (int u = 0; u < VEC; ++u) {
+      const uint32_t e = e0 + u;
+      const uint32_t t = e - fastdiv(e, g.last_div) * g.last;
+      const int64_t q = (int64_t)P[t * g.p_stride];
+      int64_t sum = 0;
+      if (q == 0) {
+        atomicAdd(&g.diag->zero_mod, 1ull);
+      } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) sum = running_step(sum, (int64_t)in.x[u * D + k], q);
+      }
+      out.x[u] = (T)sum;
+    }
+    R[v] = out.w;
+  }
+}
+
+template <typename T>
+static bool launch_blocks(const BlockSumArgs &g, int64_t D, int grid) {
+  switch (D) {
+    case 2: axis_modsum_blocks_kernel<T, 2><<<grid, 256, 0, stream()>>>(g); return true;
+    case 3: axis_modsum_blocks_kernel<T, 3><<<grid, 256, 0, stream()>>>(g); return true;
+    case 4: axis_modsum_blocks_kernel<T, 4><<<grid, 256, 0, stream()>>>(g); return true;
+    default: return false;
+  }
+}
+
 static int axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_tensor *r, int64_t axis) {
   clear_error();
   HEAL_CHECK(check_desc(a, "a", true));
@@ -167,7 +232,29 @@ static int axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_te
       if (r->dims[i] >= (int64_t)UINT32_MAX) g.fast = 0;
       else g.fd[i] = fastdiv_make((uint32_t)std::max<int64_t>(r->dims[i], 1));
     }
-    if (r->dtype == HEAL_INT32)
+    // contiguous blocks: a unit-stride reduced axis of 2..4 elements, a's other
+    // axes D times the strides of a dense row-major result, 16-byte aligned
+    const int es = elem_size(r->dtype), vec = 16 / es;
+    const int64_t D = g.ax_len;
+    bool blocks = g.ax_stride == 1 && D >= 2 && D <= 4 && r->ndim > 0 && dense_rowmajor(*r) && n % vec == 0 &&
+                  n < (int64_t)UINT32_MAX && (uintptr_t)A.data % 16 == 0 && (uintptr_t)r->data % 16 == 0;
+    for (int i = 0; i < r->ndim && blocks; ++i) blocks = r->dims[i] == 1 || g.ai.strides[i] == D * r->strides[i];
+    if (blocks) {
+      BlockSumArgs bg;
+      bg.a = A.data;
+      bg.p = P.data;
+      bg.out = r->data;
+      bg.nvec = n / vec;
+      bg.p_stride = P.strides[0];
+      bg.last = (uint32_t)r->dims[r->ndim - 1];
+      bg.last_div = fastdiv_make(bg.last);
+      bg.diag = g.diag;
+      const int grid = grid_for(bg.nvec, 256, 8);
+      blocks = r->dtype == HEAL_INT32 ? launch_blocks<int32_t>(bg, D, grid) : launch_blocks<int64_t>(bg, D, grid);
+    }
+    if (blocks) {
+      // launched above
+    } else if (r->dtype == HEAL_INT32)
       axis_modsum_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
     else
       axis_modsum_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);

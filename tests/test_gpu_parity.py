@@ -334,3 +334,21 @@ def test_cfg4_int32_31bit_columns_vs_oracle():
     fw = ntt(a, p, perm, tw)
     assert np.array_equal(fw, O.ntt(a, p, perm, tw, exact=1))
     assert np.array_equal(intt(fw, p, perm, itw, minv), a)
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+@pytest.mark.parametrize("D", [2, 3, 4, 5])
+def test_axis_modsum_over_innermost_digits(dt, D):
+    """The digit axis of a [.., L, D] tensor moved before L: each output sums
+    D adjacent values (the contiguous-block path for D <= 4), including
+    negative and out-of-range values."""
+    rng = np.random.default_rng(D)
+    n, L = 64, 6
+    p = np.array([97, 65521, 7, 3, 1 << 20 | 7, 2 ** 30 - 35][:L], dtype=dt)
+    a = rng.integers(-50, 2 ** 30, size=(2, n, 1, L, D)).astype(dt)
+    a[0, 3, 0, 2, :] = -9
+    moved = np.moveaxis(a, 4, 3)                            # [2, n, 1, D, L], digits innermost in memory
+    dev = capi.DeviceArray.from_numpy(a).reshape((2, n, 1, L, D)).moveaxis(4, 3)
+    out = capi.DeviceArray.empty((2, n, 1, L), dt)
+    capi.call("heal_axis_modsum", dev, up(p), out, 3)
+    assert np.array_equal(out.numpy(), O.axis_modsum(np.ascontiguousarray(moved), p, 3))
