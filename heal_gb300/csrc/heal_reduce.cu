@@ -295,43 +295,56 @@ __device__ __forceinline__ uint64_t gdec_digit(int64_t value, uint64_t d, uint64
 }
 
 // Dense layout, power PW <= 8: each thread decomposes the VEC elements of one
-// 16-byte vector and writes their VEC * PW digits as PW 16-byte stores.
+// 16-byte vector.  A warp stages the digits of its 32 vectors in shared
+// memory and writes them back as contiguous 512-byte runs (a thread's own
+// VEC * PW digits sit 16 * PW bytes apart from its neighbour's).
 template <typename T, int PW>
 __global__ void __launch_bounds__(256) gdec_vec_kernel(const __grid_constant__ GdecArgs g) {
   typedef typename std::conditional<sizeof(T) == 8, longlong2, int4>::type V;
   constexpr int VEC = 16 / sizeof(T);
+  __shared__ __align__(16) T stage[8][32 * VEC * PW];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T *st = stage[warp];
   const T *A = (const T *)g.in;
   T *R = (T *)g.out;
   const uint64_t mask = g.bits >= 64 ? ~0ull : ((1ull << g.bits) - 1);
   const int64_t nvec = g.n / VEC;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += (int64_t)gridDim.x * blockDim.x) {
-    T x[VEC], out[VEC * PW];
-    *(V *)x = *(const V *)(A + v * VEC);
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t v0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * 32; v0 < nvec; v0 += nwarps * 32) {
+    const int64_t v = v0 + lane;
+    const int valid = (int)(nvec - v0 < 32 ? nvec - v0 : 32);
+    if (v < nvec) {
+      T x[VEC], out[VEC * PW];
+      *(V *)x = *(const V *)(A + v * VEC);
 #pragma unroll
-    for (int e = 0; e < VEC; ++e) {
+      for (int e = 0; e < VEC; ++e) {
 #pragma unroll
-      for (int d = 0; d < PW; ++d) out[e * PW + d] = (T)(int64_t)gdec_digit<T>((int64_t)x[e], d, g.bits, mask);
-      const int64_t rest = (int64_t)gdec_digit<T>((int64_t)x[e], PW, g.bits, ~0ull);
-      // the residual after PW steps, as the reference's `value > 0` sees it
-      const int64_t resid = sizeof(T) == 4 ? (int64_t)(int32_t)(uint32_t)rest : rest;
-      if (resid > 0) {
-        unsigned long long slot = atomicAdd(&g.diag->count, 1ull);
-        if (slot < (unsigned long long)kDiagRecords) {
-          DiagRecord &rec = g.diag->rec[slot];
-          int64_t rem = v * VEC + e;
-          for (int i = g.a.ndim - 1; i >= 0; --i) {
-            rec.coord[i] = rem % g.a.dims[i];
-            rem /= g.a.dims[i];
+        for (int d = 0; d < PW; ++d) out[e * PW + d] = (T)(int64_t)gdec_digit<T>((int64_t)x[e], d, g.bits, mask);
+        const int64_t rest = (int64_t)gdec_digit<T>((int64_t)x[e], PW, g.bits, ~0ull);
+        // the residual after PW steps, as the reference's `value > 0` sees it
+        const int64_t resid = sizeof(T) == 4 ? (int64_t)(int32_t)(uint32_t)rest : rest;
+        if (resid > 0) {
+          unsigned long long slot = atomicAdd(&g.diag->count, 1ull);
+          if (slot < (unsigned long long)kDiagRecords) {
+            DiagRecord &rec = g.diag->rec[slot];
+            int64_t rem = v * VEC + e;
+            for (int i = g.a.ndim - 1; i >= 0; --i) {
+              rec.coord[i] = rem % g.a.dims[i];
+              rem /= g.a.dims[i];
+            }
+            rec.ndim = g.a.ndim;
+            rec.kind = 1;
+            rec.base_bits = g.bits;
+            rec.power = g.power;
           }
-          rec.ndim = g.a.ndim;
-          rec.kind = 1;
-          rec.base_bits = g.bits;
-          rec.power = g.power;
         }
       }
-    }
 #pragma unroll
-    for (int k = 0; k < PW; ++k) *(V *)(R + v * VEC * PW + k * VEC) = *(const V *)(out + k * VEC);
+      for (int k = 0; k < PW; ++k) *(V *)(st + (lane * PW + k) * VEC) = *(const V *)(out + k * VEC);
+    }
+    __syncwarp();
+    for (int j = lane; j < valid * PW; j += 32) *(V *)(R + (v0 * PW + j) * VEC) = *(const V *)(st + j * VEC);
+    __syncwarp();
   }
 }
 
@@ -474,7 +487,8 @@ __device__ __forceinline__ int64_t perm_at(const PermuteArgs &g, int64_t e, int6
                                      : ((const int64_t *)g.perms)[e * g.ps0 + pm * g.ps1];
 }
 
-// row-major a and result: idx = (pre * m + pm) * post + inner
+// row-major a and result: idx = (pre * m + pm) * post + inner, in units of T
+// (an element, or a 16-byte vector of a row when rows are whole vectors)
 template <typename T>
 __global__ void __launch_bounds__(256) permute_dense_kernel(const __grid_constant__ PermuteArgs g) {
   const T *A = (const T *)g.src;
@@ -628,7 +642,20 @@ static int permute(const heal_tensor *a, const heal_tensor *perms, const heal_te
       g.pa = map[pa];
       make_fast_dims(g.r, n, &g.fd);
     }
-    if (g.dense) {
+    // rows of 16-byte vectors: the gathered blocks (`post` elements) are
+    // whole aligned vectors and a vector never straddles two elementwise
+    // coordinates; the same kernel then moves one vector per index
+    const int vec = 16 / elem_size(r->dtype);
+    const bool rows = g.dense && g.fast && g.post % vec == 0 && (!g.ew_in_post || g.ew_div % vec == 0) &&
+                      (uintptr_t)A.data % 16 == 0 && (uintptr_t)r->data % 16 == 0;
+    if (rows) {
+      g.post /= vec;
+      if (g.ew_in_post) g.ew_div /= vec;
+      g.n = n / vec;
+      g.f_post = fastdiv_make((uint32_t)g.post);
+      g.f_ewdiv = fastdiv_make((uint32_t)g.ew_div);
+      permute_dense_kernel<uint4><<<grid_for(g.n, 256, 8), 256, 0, stream()>>>(g);
+    } else if (g.dense) {
       if (r->dtype == HEAL_INT32)
         permute_dense_kernel<int32_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
       else

@@ -352,3 +352,20 @@ def test_axis_modsum_over_innermost_digits(dt, D):
     out = capi.DeviceArray.empty((2, n, 1, L), dt)
     capi.call("heal_axis_modsum", dev, up(p), out, 3)
     assert np.array_equal(out.numpy(), O.axis_modsum(np.ascontiguousarray(moved), p, 3))
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+@pytest.mark.parametrize("shape,ew,pa", [
+    ((2, 64, 1, 24), 2, 1),      # the keyswitch chain's Galois permutation: whole rows
+    ((3, 32, 8), 0, 1),          # elementwise axis before the permuted one
+    ((16, 4, 6), 1, 0),          # elementwise axis inside the gathered rows
+    ((5, 32, 3), 0, 1),          # rows of 3 elements: not whole 16-byte vectors
+])
+def test_permute_row_gathers(dt, shape, ew, pa):
+    rng = np.random.default_rng(len(shape) + ew)
+    a = rng.integers(-1000, 1 << 30, size=shape).astype(dt)
+    l, m = shape[ew], shape[pa]
+    perms = np.stack([rng.permutation(m) for _ in range(l)]).astype(dt)
+    out = capi.DeviceArray.empty(shape, dt)
+    capi.call("heal_permute", up(a), up(perms), out, ew, pa)
+    assert np.array_equal(out.numpy(), O.permute(a, perms, ew, pa))
