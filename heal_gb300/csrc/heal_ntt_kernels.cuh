@@ -459,8 +459,14 @@ __device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::
   }
 }
 
+// minimum resident 512-thread CTAs per SM the register allocation must allow
+// (2, at most 64 registers, measured fastest: 1 lets some kernels take more
+// registers and fewer warps, 3 caps at 40 registers and spills)
+#ifndef HEAL_NTT_MINB
+#define HEAL_NTT_MINB 2
+#endif
 template <typename T, int MODE, bool INV, int LOGP>
-__global__ void __launch_bounds__(512) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
+__global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
   constexpr bool WIDE = MODE == MODE_W64_LAZY;
   constexpr bool LAZY = MODE != MODE_N32;
   constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
