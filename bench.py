@@ -73,18 +73,60 @@ def whole_job_rate(units_per_rank: float, world: int, ms: float) -> float:
 
 
 class Clocks:
-    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+    """Samples SM clocks and clock-event (throttle) reasons while running:
+    NVML through ctypes every 2 ms (read-only queries), else nvidia-smi every
+    200 ms."""
 
+    # NVML clocks-event reason bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu: int):
-        self.gpu = gpu
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [x for x in vis.split(",") if x.strip()]
+        self.gpu = int(ids[gpu]) if gpu < len(ids) and ids[gpu].strip().isdigit() else gpu
         self.proc = None
         self.path = None
+        self.nvml = None
+        self.rows = []
+
+    def _nvml_open(self):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        h = ctypes.c_void_p()
+        if lib.nvmlInit_v2() != 0 or lib.nvmlDeviceGetHandleByIndex_v2(self.gpu, ctypes.byref(h)) != 0:
+            return None
+        fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        return lib, h, fn
+
+    def _sample_loop(self):
+        import ctypes
+        lib, h, reasons_fn = self.nvml
+        mhz, mx, mw, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))          # NVML_CLOCK_SM
+        while not self.stop.is_set():
+            ok = lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0
+            ok = ok and reasons_fn(h, ctypes.byref(rs)) == 0
+            p = mw.value if lib.nvmlDeviceGetPowerUsage(h, ctypes.byref(mw)) == 0 else 0
+            if ok:
+                self.rows.append((mhz.value, mx.value, p / 1000.0, rs.value))
+            self.stop.wait(0.002)
 
     def __enter__(self):
+        import threading
+        self.nvml = self._nvml_open()
+        if self.nvml:
+            self.stop = threading.Event()
+            self.thread = threading.Thread(target=self._sample_loop, daemon=True)
+            self.thread.start()
+            return self
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
@@ -96,11 +138,22 @@ class Clocks:
         return self
 
     def __exit__(self, *exc):
+        if self.nvml:
+            self.stop.set()
+            self.thread.join()
         if self.proc:
             self.proc.terminate()
             self.proc.wait()
 
     def summary(self):
+        if self.nvml:
+            if not self.rows:
+                return {"sm_mhz": None, "sm_max_mhz": None, "samples": 0, "reasons": ["no NVML samples"],
+                        "source": "nvml"}
+            reasons = sorted({name for r in self.rows for bit, name in self.REASONS.items() if r[3] & bit})
+            return {"sm_mhz": statistics.median(r[0] for r in self.rows), "sm_max_mhz": float(self.rows[0][1]),
+                    "power_w": statistics.median(r[2] for r in self.rows), "samples": len(self.rows),
+                    "reasons": reasons, "source": "nvml, every 2 ms"}
         rows = []
         try:
             for line in open(self.path):
@@ -116,7 +169,7 @@ class Clocks:
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
-                "samples": len(rows), "reasons": reasons}
+                "samples": len(rows), "reasons": reasons, "source": "nvidia-smi, every 200 ms"}
 
 
 def peaks():
