@@ -507,7 +507,7 @@ def cfg4_config(args, timed):
 def ragged_config(args, timed):
     """cfg3: 256 ciphertexts of mixed ring degree and limb count, the cfg1
     chain on each; plain loop (default and autotuned NTT plans) against one
-    CUDA graph (1 branch, and 16 parallel branches)."""
+    CUDA graph (1 branch, and 8 parallel branches: 8 to 64 measured within 10%, 8 fastest)."""
     import hashlib
     from heal_gb300 import capi
     from heal_gb300.configs import Cfg3
@@ -526,7 +526,7 @@ def ragged_config(args, timed):
     digest = lambda: hashlib.sha256(b"".join(np.ascontiguousarray(a.numpy()).tobytes() for a in c3.AS)).hexdigest()
     want = digest()
     res = {}
-    for nb in (1, 16):
+    for nb in (1, 8):
         g = c3.graph(nb)
         for a in c3.AS:                                # the replay must rewrite every output
             capi.call("heal_copy_strided", capi.DeviceArray.from_numpy(np.zeros(a.shape, np.int64)), a)
@@ -536,7 +536,7 @@ def ragged_config(args, timed):
         res[nb] = (ms / steps, launches / steps, same)
         del g
     round_trip = all(np.array_equal(c3.RA[i].numpy(), c3.A[i].numpy()) for i in range(len(c3.specs)))
-    best = min(res[1][0], res[16][0])
+    best = min(res[1][0], res[8][0])
     shapes = sorted(plans)
     return {"workload": "256 ciphertexts [2, N, 1, L] int64, N in 2^12..2^16, L uniform in 2..32, 30-bit primes; "
                         "ntt(A), ntt(B), intt(ntt(A)), modmul, axis_modsum per ciphertext (1280 calls per step)",
@@ -544,13 +544,13 @@ def ragged_config(args, timed):
             "elements_per_tensor_set": c3.elements(),
             "step_ms_plain_default_plans": ms_default / steps,
             "step_ms_plain_tuned_plans": ms_tuned / steps,
-            "step_ms_graph_1_branch": res[1][0], "step_ms_graph_16_branches": res[16][0],
+            "step_ms_graph_1_branch": res[1][0], "step_ms_graph_8_branches": res[8][0],
             "graph_speedup_vs_plain": (ms_default / steps) / best,
             "ciphertexts_per_s": len(c3.specs) / (best / 1e3),
             "transform_limbs_per_s": c3.transform_limbs() / (best / 1e3),
             "hbm_frac": c3.bytes_per_step() / (best / 1e3) / 1e9 / hbm,
-            "launches_per_step": res[16][1], "plain_launches_per_step": l_plain / steps,
-            "graph_equals_loop": res[1][2] and res[16][2], "round_trip_exact": round_trip,
+            "launches_per_step": res[8][1], "plain_launches_per_step": l_plain / steps,
+            "graph_equals_loop": res[1][2] and res[8][2], "round_trip_exact": round_trip,
             "autotuned_shapes": len(shapes), "autotune_s": tune_s, "setup_s": setup_s,
             "plans_sample": {f"{n}x{l}": {"fwd": plans[(n, l)][0], "inv": plans[(n, l)][1]}
                              for n, l in shapes[:: max(1, len(shapes) // 6)]}}

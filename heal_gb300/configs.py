@@ -150,7 +150,7 @@ class Cfg3:
             branch(-1)
         return rec
 
-    def graph(self, branches: int = 16) -> capi.Graph:
+    def graph(self, branches: int = 8) -> capi.Graph:
         return capi.Graph(self.record(branches), branches=branches)
 
     def autotune(self, reps: int = 3) -> dict:
