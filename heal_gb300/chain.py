@@ -50,6 +50,21 @@ class KeyswitchChain:
     def shape(self):
         return (2, self.n, 1, self.L)
 
+    def twin(self) -> "KeyswitchChain":
+        """A chain on the same resident tables and key with its own
+        intermediate tensors, so that two chains can run on two streams."""
+        t = object.__new__(KeyswitchChain)
+        t.__dict__.update(self.__dict__)
+        E = capi.DeviceArray.empty
+        n, L, D = self.n, self.L, self.D
+        t.x = E((2, n, 1, L), self.dtype, zero=False)
+        t.dig = E((2, n, 1, L, D), self.dtype, zero=False)
+        t.dn = E((2, n, 1, L * D), self.dtype, zero=False)
+        t.acc = E((2, n, 1, L), self.dtype, zero=False)
+        t.dig_flat = t.dig.reshape((2, n, 1, L * D))
+        t.prod_moved = t.dn.reshape((2, n, 1, L, D)).moveaxis(4, 3)
+        return t
+
     def tune(self, ct: capi.DeviceArray, reps: int = 5) -> dict:
         """Runs the NTT autotuner on the chain's two transform shapes (the
         INTT of the ciphertext, the NTT of the digits) and keeps the fastest
