@@ -369,3 +369,23 @@ def test_permute_row_gathers(dt, shape, ew, pa):
     out = capi.DeviceArray.empty(shape, dt)
     capi.call("heal_permute", up(a), up(perms), out, ew, pa)
     assert np.array_equal(out.numpy(), O.permute(a, perms, ew, pa))
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+@pytest.mark.parametrize("n,in_place", [(1 << 18, False), ((1 << 18) + 24, True), ((1 << 20) + 8, False)])
+def test_large_dense_modops_vs_oracle(dt, n, in_place):
+    """Large dense operands (many grid-stride iterations, a length that is
+    not a multiple of the grid), in place and out of place, with moduli on
+    the last axis and signed values."""
+    rng = np.random.default_rng(n + in_place)
+    k = 24
+    p = np.array([97, 65521, 2 ** 30 - 35, 7, 3, 2 ** 31 - 1] * 4, dtype=dt)[:k]
+    shape = (n // k, k)
+    a = rng.integers(-2 ** 20, 2 ** 31 - 1, size=shape).astype(dt)
+    b = rng.integers(0, 2 ** 31 - 1, size=shape).astype(dt)
+    for name, op in (("heal_modmul_ttt", O.modmul), ("heal_modsum_ttt", O.modsum)):
+        da, db = up(a), up(b)
+        out = da if in_place else capi.DeviceArray.empty(shape, dt)
+        capi.call(name, da, db, up(p), out)
+        assert np.array_equal(out.numpy(), op(a, b, p)), name
+    capi.synchronize()
