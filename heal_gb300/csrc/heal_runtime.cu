@@ -339,6 +339,11 @@ int materialize(const heal_tensor &t_in, heal_tensor *out, void **owned) {
 // stay valid while the write generations of those tensors' allocations do.
 // Memory not allocated by heal_alloc has no generation: its entries are
 // rebuilt on every use (the previous buffer is freed stream-ordered).
+//
+// Streams: an entry records an event on the stream that built it and the
+// streams that have used it.  A lookup from another stream first waits for
+// that event (the build may still be running there); dropping an entry that
+// another stream has used waits for the device before its buffers are freed.
 struct CacheEntry {
   std::vector<std::pair<const void *, uint64_t>> deps;
   uint64_t epoch = 0;
@@ -346,6 +351,9 @@ struct CacheEntry {
   int64_t i0 = 0, i1 = 0;
   bool b0 = false, b1 = false;
   uint64_t used = 0;
+  cudaEvent_t ready = nullptr;        // recorded after the build was enqueued
+  std::vector<cudaStream_t> users;    // streams that have used the tables
+  bool complete = false;              // false while (or if) the build did not finish
 };
 static std::unordered_map<std::string, CacheEntry> g_cache;
 static uint64_t g_cache_clock = 0;
@@ -370,8 +378,25 @@ static std::string key_of(const char *kind, std::initializer_list<const heal_ten
 }
 
 static void drop_entry(CacheEntry &e) {
+  bool foreign = !e.complete;  // another stream may still be reading (or building) the tables
+  for (cudaStream_t s : e.users) foreign = foreign || s != stream();
+  if (foreign && !e.bufs.empty()) cudaDeviceSynchronize();
   for (void *b : e.bufs) scratch_free(b);
   e.bufs.clear();
+  if (e.ready) cudaEventDestroy(e.ready);
+  e.ready = nullptr;
+  e.users.clear();
+}
+
+// Called once an entry's build is enqueued on the current stream.
+static void entry_built(CacheEntry &e) {
+  if (!e.ready && cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    e.ready = nullptr;
+  }
+  if (e.ready) cudaEventRecord(e.ready, stream());
+  e.users.assign(1, stream());
+  e.complete = true;
 }
 
 static int refuse_in_capture(const char *what) {
@@ -385,7 +410,8 @@ static int refuse_in_capture(const char *what) {
 static CacheEntry *cache_lookup(const std::string &key) {
   auto it = g_cache.find(key);
   if (it == g_cache.end()) return nullptr;
-  bool ok = true;
+  bool ok = it->second.complete;  // a build that returned early left an incomplete entry
+  if (!ok && g_rt.capturing) return nullptr;
   for (auto &d : it->second.deps) {
     uint64_t g = generation_of(d.first);
     if (g != d.second || (g == 0 && it->second.epoch != g_epoch.load())) ok = false;
@@ -396,8 +422,14 @@ static CacheEntry *cache_lookup(const std::string &key) {
     g_cache.erase(it);
     return nullptr;
   }
-  it->second.used = ++g_cache_clock;
-  return &it->second;
+  CacheEntry &e = it->second;
+  e.used = ++g_cache_clock;
+  const cudaStream_t s = stream();
+  if (!g_rt.capturing && std::find(e.users.begin(), e.users.end(), s) == e.users.end()) {
+    if (e.ready) cudaStreamWaitEvent(s, e.ready, 0);  // the build may still run on its own stream
+    e.users.push_back(s);
+  }
+  return &e;
 }
 
 static CacheEntry &cache_insert(const std::string &key, std::initializer_list<const void *> deps) {
@@ -478,6 +510,7 @@ int mod_table(const heal_tensor &p, ModTable *out) {
       mod_table_kernel<<<grid_for(cnt, 128), 128, 0, stream()>>>(p.data, p.dtype, make_view(p), cnt, buf);
       HEAL_CHECK(check_launch("mod_table"));
     }
+    entry_built(n);
     e = &n;
   }
   out->consts = e->bufs[0];
@@ -525,6 +558,7 @@ int mod_info(const heal_tensor &p, ModInfo *out) {
     scratch_free(mmb);
     n.i0 = k ? dec64(h.min_enc) : 1;
     n.i1 = k ? dec64(h.max_enc) : 1;
+    entry_built(n);
     e = &n;
   }
   out->min_q = e->i0;
@@ -698,6 +732,7 @@ int twiddle_table(const heal_tensor &tw, const heal_tensor &p, int wide, Twiddle
     HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
     scratch_free(rows_d);
     n.i0 = (int64_t)rows.size();
+    entry_built(n);
     e = &n;
   }
   out->pairs = e->bufs[0];
@@ -716,6 +751,7 @@ int minv_table(const heal_tensor &minv, const heal_tensor &p, int64_t k, int wid
   if (!e) {
     CacheEntry &n = cache_insert(key, {minv.data, p.data});
     HEAL_CHECK(build_pairs(minv.data, minv.dtype, minv.strides[0], 0, mi.q, nullptr, k, 1, wide, n));
+    entry_built(n);
     e = &n;
   }
   out->pairs = e->bufs[0];
@@ -773,6 +809,7 @@ int perm_info(const heal_tensor &perm, PermInfo *out) {
     scratch_free(cnt);
     n.b0 = h.distinct == (unsigned long long)m && h.bad == 0;
     n.b1 = h.bad != 0;
+    entry_built(n);
     e = &n;
   }
   out->perm32 = (const int32_t *)e->bufs[0];
@@ -814,6 +851,7 @@ int perms_valid(const heal_tensor &perms, int64_t m, bool *ok) {
     HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
     scratch_free(cnt);
     n.b0 = h == 0;
+    entry_built(n);
     e = &n;
   }
   *ok = e->b0;
