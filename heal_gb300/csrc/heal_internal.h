@@ -105,12 +105,14 @@ int twiddle_table(const heal_tensor &tw, const heal_tensor &p, int wide, Twiddle
 int minv_table(const heal_tensor &minv, const heal_tensor &p, int64_t k, int wide, TwiddleTable *out);
 
 // A permutation [m] validated once: perm32[u], inv32[v] = largest u with
-// perm[u] == v (or -1), and whether it is a bijection.
+// perm[u] == v (or -1), whether it is a bijection, and whether it is the
+// bit reversal of the index (then kernels compute it instead of loading it).
 struct PermInfo {
   const int32_t *perm32;
   const int32_t *inv32;
   bool bijective;
-  bool bad;  // some index outside [0, m)
+  bool bad;        // some index outside [0, m)
+  int bitrev_log;  // log2(m) when perm[u] is the bit reversal of u over log2(m) bits (its own inverse), else 0
 };
 int perm_info(const heal_tensor &perm, PermInfo *out);
 

@@ -194,6 +194,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   base.tw_s0 = tw->strides[0];
   base.tw_s1 = tw->strides[1];
   base.q = mi.q;
+  base.bitrev = pi.bitrev_log;  // every table this call indexes is the bit reversal (its own inverse)
   if (inv) {
     base.minv_pairs = mt.pairs;
     base.minv_neg = mt.neg_flag;

@@ -57,7 +57,14 @@ struct NttArgs {
   int scale;
   int canon_load;
   int force_exact;
+  int bitrev;  // log2(m) when the permutation is the index's bit reversal (computed, not loaded), else 0
 };
+
+// row of a permutation table (load_map / store_scatter / store_gather), or
+// the bit reversal of v when the call's permutation is bit reversal
+__device__ __forceinline__ int64_t perm_row(const NttArgs &g, const int32_t *table, int64_t v) {
+  return g.bitrev ? (int64_t)(__brev((uint32_t)v) >> (32 - g.bitrev)) : (int64_t)table[v];
+}
 
 template <bool WIDE>
 struct Word;
@@ -171,7 +178,7 @@ template <typename T>
 __device__ __forceinline__ int64_t load_point(const NttArgs &g, const TileCtx &x, int s, int64_t t) {
   const int64_t v = x.row_of(g, s);
   if (g.load_map) {
-    const int32_t sr = g.load_map[v];
+    const int64_t sr = perm_row(g, g.load_map, v);
     if (sr < 0) return (int64_t)((const T *)g.old)[x.i * g.os[0] + v * g.os[1] + x.j * g.os[2] + t * g.os[3]];
     return (int64_t)((const T *)g.src)[x.i * g.ss[0] + (int64_t)sr * g.ss[1] + x.j * g.ss[2] + t * g.ss[3]];
   }
@@ -181,7 +188,7 @@ __device__ __forceinline__ int64_t load_point(const NttArgs &g, const TileCtx &x
 template <typename T>
 __device__ __forceinline__ void store_point(const NttArgs &g, const TileCtx &x, int s, int64_t t, int64_t val) {
   const int64_t v = x.row_of(g, s);
-  const int64_t dr = g.store_scatter ? (int64_t)g.store_scatter[v] : v;
+  const int64_t dr = g.store_scatter ? perm_row(g, g.store_scatter, v) : v;
   ((T *)g.dst)[x.i * g.ds[0] + dr * g.ds[1] + x.j * g.ds[2] + t * g.ds[3]] = (T)val;
 }
 
@@ -243,7 +250,7 @@ __device__ __noinline__ void exact_tile(const NttArgs &g, const TileCtx &x, int6
     const int s = e >> logC, c = e & (C - 1);
     const int64_t t = x.t0 + c;
     if (t >= g.k) continue;
-    int64_t val = g.store_gather ? tile[tidx(g.store_gather[s], c, logC)] : tile[tidx(s, c, logC)];
+    int64_t val = g.store_gather ? tile[tidx((int)perm_row(g, g.store_gather, s), c, logC)] : tile[tidx(s, c, logC)];
     if (g.scale) val = crem128((i128)val * raw_any(g.minv_raw, t * g.minv_s0, is32), g.q[t]);
     store_point<T>(g, x, s, t, val);
   }
@@ -329,7 +336,7 @@ __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ 
     const int s = e >> logC, c = e & (C - 1);
     const int64_t t = x.t0 + c;
     if (t >= g.k) continue;
-    int64_t val = g.store_gather ? tile[tidx(g.store_gather[s], c, logC)] : tile[tidx(s, c, logC)];
+    int64_t val = g.store_gather ? tile[tidx((int)perm_row(g, g.store_gather, s), c, logC)] : tile[tidx(s, c, logC)];
     if (g.scale) {
       const Pair pr = __ldg((const Pair *)g.minv_pairs + t);
       val = (int64_t)mulw<WIDE>((W)val, pr, (W)g.q[t]);
@@ -548,7 +555,7 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
 #pragma unroll
       for (int e = 0; e < kPT; ++e) {
         const int s = point_of<INV, LOGP, kLPT>(0, r, e);
-        store_point<T>(g, x, s, t, (int64_t)wt[tidx(g.store_gather[s], c, logC)]);
+        store_point<T>(g, x, s, t, (int64_t)wt[tidx((int)perm_row(g, g.store_gather, s), c, logC)]);
       }
     }
     return;

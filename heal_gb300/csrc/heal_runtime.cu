@@ -764,10 +764,11 @@ int minv_table(const heal_tensor &minv, const heal_tensor &p, int64_t k, int wid
 // ---------------------------------------------------------- permutations
 struct PermCounts {
   unsigned long long bad, distinct;
+  unsigned long long not_bitrev;  // entries differing from the bit reversal of their index
 };
 
-__global__ void perm_kernel(const void *perm, int dtype, int64_t stride, int64_t m, int32_t *perm32, int32_t *inv32,
-                            PermCounts *cnt) {
+__global__ void perm_kernel(const void *perm, int dtype, int64_t stride, int64_t m, int logm, int32_t *perm32,
+                            int32_t *inv32, PermCounts *cnt) {
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < m; u += (int64_t)gridDim.x * blockDim.x) {
     int64_t v = load_any(perm, dtype, u * stride);
     if (v < 0 || v >= m) {
@@ -778,6 +779,7 @@ __global__ void perm_kernel(const void *perm, int dtype, int64_t stride, int64_t
     perm32[u] = (int32_t)v;
     int old = atomicMax(&inv32[v], (int)u);
     if (old < 0) atomicAdd(&cnt->distinct, 1ull);
+    if (logm > 0 && v != (int64_t)(__brev((uint32_t)u) >> (32 - logm))) atomicAdd(&cnt->not_bitrev, 1ull);
   }
 }
 
@@ -799,8 +801,12 @@ int perm_info(const heal_tensor &perm, PermInfo *out) {
     HEAL_TRY_CUDA(cudaMemsetAsync(i32, 0xFF, sizeof(int32_t) * std::max<int64_t>(m, 1), stream()));
     HEAL_TRY_CUDA(cudaMemsetAsync(cnt, 0, sizeof(PermCounts), stream()));
     if (m) {
-      perm_kernel<<<grid_for(m, 256), 256, 0, stream()>>>(perm.data, perm.dtype, perm.strides[0], m, (int32_t *)p32,
-                                                           (int32_t *)i32, (PermCounts *)cnt);
+      int logm = 0;
+      while (((int64_t)1 << logm) < m) ++logm;
+      if (((int64_t)1 << logm) != m) logm = 0;  // bit reversal only for power-of-two lengths
+      perm_kernel<<<grid_for(m, 256), 256, 0, stream()>>>(perm.data, perm.dtype, perm.strides[0], m, logm,
+                                                           (int32_t *)p32, (int32_t *)i32, (PermCounts *)cnt);
+      n.i0 = logm;
       HEAL_CHECK(check_launch("perm_info"));
     }
     PermCounts h;
@@ -809,6 +815,7 @@ int perm_info(const heal_tensor &perm, PermInfo *out) {
     scratch_free(cnt);
     n.b0 = h.distinct == (unsigned long long)m && h.bad == 0;
     n.b1 = h.bad != 0;
+    n.i1 = (m > 1 && n.i0 > 0 && n.b0 && h.not_bitrev == 0) ? n.i0 : 0;
     entry_built(n);
     e = &n;
   }
@@ -816,6 +823,7 @@ int perm_info(const heal_tensor &perm, PermInfo *out) {
   out->inv32 = (const int32_t *)e->bufs[1];
   out->bijective = e->b0;
   out->bad = e->b1;
+  out->bitrev_log = (int)e->i1;
   return HEAL_OK;
 }
 

@@ -389,3 +389,19 @@ def test_large_dense_modops_vs_oracle(dt, n, in_place):
         capi.call(name, da, db, up(p), out)
         assert np.array_equal(out.numpy(), op(a, b, p)), name
     capi.synchronize()
+
+
+@pytest.mark.parametrize("m", [16, 4096, 1 << 14])
+def test_ntt_permutation_one_swap_from_bit_reversal(m):
+    """A permutation that differs from bit reversal in two entries must not be
+    taken for it (the kernels compute bit reversal instead of loading it)."""
+    k = 3
+    qs = P.ntt_primes(1 << 50, m, k)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m)
+    swapped = perm.copy()
+    swapped[[1, m - 2]] = swapped[[m - 2, 1]]
+    x = P.residues(m, (2, m, 1, k), qs)
+    for pm in (perm, swapped):
+        assert np.array_equal(ntt(x, p, pm, tw), O.ntt(x, p, pm, tw))
+        y = O.ntt(x, p, pm, tw)
+        assert np.array_equal(intt(y, p, pm, itw, minv), O.intt(y, p, pm, itw, minv))
