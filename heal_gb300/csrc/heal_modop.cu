@@ -40,6 +40,8 @@ struct ModopArgs {
   int64_t last;        // result's last dimension (dense kernel)
   FastDiv last_div;    // division by `last` (dense kernel, n < 2^32)
   int p_per_last;      // dense kernel: modulus index = coordinate on the last axis
+  int b_stream;        // dense kernel, in-place update r = a op b: b is loaded evict-first so that the
+                       // updated tensor (read next) keeps its place in L2
   FastDims fd;         // general kernel: 32-bit decomposition of r's coordinates
   Diag *diag;
 };
@@ -166,8 +168,13 @@ __global__ void __launch_bounds__(256) modop_dense_kernel(const __grid_constant_
       *(V *)a0 = *(const V *)(A + v * VEC);
       *(V *)a1 = *(const V *)(A + (v + stride) * VEC);
       if (B) {
-        *(V *)b0 = *(const V *)(B + v * VEC);
-        *(V *)b1 = *(const V *)(B + (v + stride) * VEC);
+        if (g.b_stream) {
+          *(V *)b0 = __ldcs((const V *)(B + v * VEC));
+          *(V *)b1 = __ldcs((const V *)(B + (v + stride) * VEC));
+        } else {
+          *(V *)b0 = *(const V *)(B + v * VEC);
+          *(V *)b1 = *(const V *)(B + (v + stride) * VEC);
+        }
       }
     }
     compute(v * VEC, a0, b0, r0);
@@ -466,6 +473,7 @@ static int modop(int op, const heal_tensor *a, const heal_tensor *b, int64_t bs,
     }
     if (dense && g.last > 0 && g.last < (int64_t)UINT32_MAX) g.last_div = fastdiv_make((uint32_t)g.last);
     else dense = dense && !g.p_per_last;
+    g.b_stream = dense && b && A.data == r->data && B.data != r->data;
     if (!dense) {
       // general kernel: merge axes that every operand walks linearly
       View *vs[4] = {&g.r, &g.a, &g.b, &g.pd};
