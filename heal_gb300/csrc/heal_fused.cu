@@ -98,7 +98,10 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
     int64_t a0 = 0, b0 = 0, r0 = 0, t = 0, cp = 0, cp2 = 0;
     if (g.fd.fast) {
       uint32_t rem = (uint32_t)idx;
-      for (int i = g.r.ndim - 1; i >= 0; --i) {
+#pragma unroll
+      for (int k = 0; k < HEAL_MAX_DIMS; ++k) {  // unrolled: per-axis parameters at fixed offsets
+        const int i = HEAL_MAX_DIMS - 1 - k;
+        if (i >= g.r.ndim) continue;
         const uint32_t qd = fastdiv(rem, g.fd.fd[i]);
         const int64_t c = rem - qd * (uint32_t)g.r.dims[i];
         rem = qd;

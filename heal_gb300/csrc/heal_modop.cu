@@ -8,11 +8,13 @@
 // axes).  Non-negative operands with a positive modulus take the fast paths
 // of heal_arith.h; anything else takes the exact double-width `%`.
 //
-// Two kernels: a dense kernel (result, a and b row-major with the same
+// Three kernels: a dense kernel (result, a and b row-major with the same
 // shape, p a scalar or a [k] vector on the last axis — every call of the
-// keyswitch chain) that streams 16-byte vectors, and a general strided
-// kernel.  Both are HBM-bound: per element they move sizeof(T) x (reads of
-// a and b + one write).
+// keyswitch chain) that streams 16-byte vectors; a vector kernel for a
+// result contiguous on its innermost axis with operands contiguous or
+// broadcast there (16-byte units, one coordinate decomposition each); and a
+// general strided kernel.  All are HBM-bound: per element they move
+// sizeof(T) x (reads of a and b + one write), less for broadcast operands.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,6 +45,8 @@ struct ModopArgs {
   int b_stream;        // dense kernel, in-place update r = a op b: b is loaded evict-first so that the
                        // updated tensor (read next) keeps its place in L2
   FastDims fd;         // general kernel: 32-bit decomposition of r's coordinates
+  int vs_a, vs_b, vs_pd;  // vector kernel: innermost stride (0 or 1) of a, b and the modulus index
+  int off32;              // vector kernel: every offset fits 32 bits
   Diag *diag;
 };
 
@@ -234,7 +238,10 @@ __global__ void __launch_bounds__(256) modop_general_kernel(const __grid_constan
       if (idx >= g.n) continue;
       if (g.fd.fast) {
         uint32_t rem = (uint32_t)idx;
-        for (int i = g.r.ndim - 1; i >= 0; --i) {
+#pragma unroll
+        for (int k = 0; k < HEAL_MAX_DIMS; ++k) {  // unrolled: per-axis parameters at fixed offsets
+          const int i = HEAL_MAX_DIMS - 1 - k;
+          if (i >= g.r.ndim) continue;
           const uint32_t q = fastdiv(rem, g.fd.fd[i]);
           const int64_t c = rem - q * (uint32_t)g.r.dims[i];
           rem = q;
@@ -269,6 +276,92 @@ __global__ void __launch_bounds__(256) modop_general_kernel(const __grid_constan
     for (int u = 0; u < kGenU; ++u)
       if (base + (int64_t)u * blockDim.x < g.n)
         R[orr[u]] = elem_op<T, OP>(av[u], bv[u], q_of<T>(g, cv[u]), cv[u], g.diag);
+  }
+}
+
+// ------------------------------------------------ vector kernel
+// The general kernel's work in units of VEC elements of the innermost axis
+// (16 bytes of result): a result that is contiguous there, with operands
+// that are contiguous (vector loads) or broadcast (one load) along it — a
+// plaintext or diagonal broadcast over the ciphertext's polynomials or
+// slots.  The views hold the innermost axis divided by VEC, with its strides
+// multiplied by VEC, so one decomposition gives a unit's first element; its
+// other elements follow at vs_* apart.
+constexpr int kVecU = 4;
+
+template <typename T, int OP, int VEC, typename Off>
+__global__ void __launch_bounds__(256) modop_vec_kernel(const __grid_constant__ ModopArgs g) {
+  typedef typename VecOf<T>::type V;
+  typedef typename MGOf<T>::type M;
+  const T *A = (const T *)g.ap;
+  const T *B = (const T *)g.bp;
+  T *R = (T *)g.rp;
+  const int64_t units = g.n / VEC;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x * kVecU;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * kVecU + threadIdx.x; base < units; base += step) {
+    Off oa[kVecU], ob[kVecU], orr[kVecU], opd[kVecU];
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t idx = base + (int64_t)u * blockDim.x;
+      oa[u] = ob[u] = orr[u] = opd[u] = 0;
+      if (idx >= units) continue;
+      if (g.fd.fast) {
+        uint32_t rem = (uint32_t)idx;
+#pragma unroll
+        for (int k = 0; k < HEAL_MAX_DIMS; ++k) {  // unrolled: per-axis parameters at fixed offsets
+          const int i = HEAL_MAX_DIMS - 1 - k;
+          if (i >= g.r.ndim) continue;
+          const uint32_t q = fastdiv(rem, g.fd.fd[i]);
+          const Off c = (Off)(rem - q * (uint32_t)g.r.dims[i]);
+          rem = q;
+          oa[u] += c * (Off)g.a.strides[i];
+          ob[u] += c * (Off)g.b.strides[i];
+          opd[u] += c * (Off)g.pd.strides[i];
+          orr[u] += c * (Off)g.r.strides[i];
+        }
+      } else {
+        int64_t rem = idx;
+        for (int i = g.r.ndim - 1; i >= 0; --i) {
+          const int64_t c = rem % g.r.dims[i];
+          rem /= g.r.dims[i];
+          oa[u] += (Off)(c * g.a.strides[i]);
+          ob[u] += (Off)(c * g.b.strides[i]);
+          opd[u] += (Off)(c * g.pd.strides[i]);
+          orr[u] += (Off)(c * g.r.strides[i]);
+        }
+      }
+    }
+    T av[kVecU][VEC], bv[kVecU][VEC];
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      if (base + (int64_t)u * blockDim.x >= units) continue;
+      if (g.vs_a) {
+        *(V *)av[u] = *(const V *)(A + oa[u]);
+      } else {
+        const T x = A[oa[u]];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) av[u][j] = x;
+      }
+      if (B && g.vs_b) {
+        *(V *)bv[u] = *(const V *)(B + ob[u]);
+      } else {
+        const T x = B ? B[ob[u]] : (T)g.bs;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) bv[u][j] = x;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      if (base + (int64_t)u * blockDim.x >= units) continue;
+      T rv[VEC];
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) {
+        const M c = mg_of<T>(g, opd[u] + j * g.vs_pd);
+        const int64_t b = B ? (int64_t)bv[u][j] : g.bs;
+        rv[j] = elem_op<T, OP>((int64_t)av[u][j], b, q_of<T>(g, c), c, g.diag);
+      }
+      *(V *)(R + orr[u]) = *(const V *)rv;
+    }
   }
 }
 
@@ -366,6 +459,30 @@ static int64_t hoist_blocks(int64_t last, int vec, int64_t want) {
   return (want / unit) * unit;
 }
 
+// Switches merged general-kernel views to the vector kernel's units when
+// the result is contiguous on its innermost axis and each operand is
+// contiguous (in aligned 16-byte vectors) or broadcast there.
+static bool vector_units(ModopArgs &g, size_t elem) {
+  const int vec = (int)(16 / elem);
+  const int in = g.r.ndim - 1;
+  if (in < 0 || !inner_vectors(g.r, vec, g.rp, elem)) return false;
+  auto operand = [&](const View &v, const void *base) {
+    return v.strides[in] == 0 || inner_vectors(v, vec, base, elem);
+  };
+  if (!operand(g.a, g.ap) || (g.bp && !operand(g.b, g.bp))) return false;
+  if (g.pd.strides[in] != 0 && g.pd.strides[in] != 1) return false;
+  g.off32 = view_off32(g.r) && view_off32(g.a) && view_off32(g.b) && view_off32(g.pd);
+  g.vs_a = (int)g.a.strides[in];
+  g.vs_b = g.bp ? (int)g.b.strides[in] : 0;
+  g.vs_pd = (int)g.pd.strides[in];
+  View *vs[5] = {&g.r, &g.a, &g.b, &g.p, &g.pd};
+  for (View *v : vs) {
+    v->dims[in] /= vec;
+    v->strides[in] *= vec;
+  }
+  return true;
+}
+
 template <typename T, int OP, int VEC>
 static void launch_dense(ModopArgs &g, cudaStream_t s, int64_t want_blocks) {
   const int64_t vecs = (g.n / VEC + 1) / 2 + 1;  // two vectors per thread per iteration
@@ -377,10 +494,19 @@ static void launch_dense(ModopArgs &g, cudaStream_t s, int64_t want_blocks) {
     modop_dense_kernel<T, OP, VEC, false><<<(unsigned)want, 256, 0, s>>>(g);
 }
 
+enum Kind { KIND_GENERAL = 0, KIND_DENSE = 1, KIND_VEC = 2 };
+
 template <typename T, int OP>
-static int launch(ModopArgs &g, bool dense) {
+static int launch(ModopArgs &g, int kind) {
   cudaStream_t s = stream();
-  if (dense) {
+  if (kind == KIND_VEC) {
+    constexpr int VEC = 16 / sizeof(T);
+    const int grid = grid_for((g.n / VEC + kVecU - 1) / kVecU, 256, 8);
+    if (g.off32)
+      modop_vec_kernel<T, OP, VEC, int32_t><<<grid, 256, 0, s>>>(g);
+    else
+      modop_vec_kernel<T, OP, VEC, int64_t><<<grid, 256, 0, s>>>(g);
+  } else if (kind == KIND_DENSE) {
     bool aligned = ((uintptr_t)g.ap % 16 == 0) && ((uintptr_t)g.rp % 16 == 0) && (!g.bp || (uintptr_t)g.bp % 16 == 0);
     const int64_t want = (int64_t)std::max(device_sm_count(), 1) * 8;
     if (aligned)
@@ -474,21 +600,24 @@ static int modop(int op, const heal_tensor *a, const heal_tensor *b, int64_t bs,
     if (dense && g.last > 0 && g.last < (int64_t)UINT32_MAX) g.last_div = fastdiv_make((uint32_t)g.last);
     else dense = dense && !g.p_per_last;
     g.b_stream = dense && b && A.data == r->data && B.data != r->data;
+    int kind = dense ? KIND_DENSE : KIND_GENERAL;
     if (!dense) {
       // general kernel: merge axes that every operand walks linearly
       View *vs[4] = {&g.r, &g.a, &g.b, &g.pd};
       coalesce_views(vs, 4, 0u, nullptr);
-      make_fast_dims(g.r, n, &g.fd);
+      if (vector_units(g, elem_size(dt))) kind = KIND_VEC;
+      make_fast_dims(g.r, kind == KIND_VEC ? n / (16 / elem_size(dt)) : n, &g.fd);
+      g.off32 = g.off32 && g.fd.fast;
     }
     if (op == OP_MOD) {
       // mod_tt / tc / ct: a and b play the roles of dividend and divisor
-      rc = dt == HEAL_INT32 ? launch<int32_t, OP_MOD>(g, dense) : launch<int64_t, OP_MOD>(g, dense);
+      rc = dt == HEAL_INT32 ? launch<int32_t, OP_MOD>(g, kind) : launch<int64_t, OP_MOD>(g, kind);
     } else if (dt == HEAL_INT32) {
-      rc = op == OP_MUL ? launch<int32_t, OP_MUL>(g, dense)
-           : op == OP_SUM ? launch<int32_t, OP_SUM>(g, dense) : launch<int32_t, OP_NEG>(g, dense);
+      rc = op == OP_MUL ? launch<int32_t, OP_MUL>(g, kind)
+           : op == OP_SUM ? launch<int32_t, OP_SUM>(g, kind) : launch<int32_t, OP_NEG>(g, kind);
     } else {
-      rc = op == OP_MUL ? launch<int64_t, OP_MUL>(g, dense)
-           : op == OP_SUM ? launch<int64_t, OP_SUM>(g, dense) : launch<int64_t, OP_NEG>(g, dense);
+      rc = op == OP_MUL ? launch<int64_t, OP_MUL>(g, kind)
+           : op == OP_SUM ? launch<int64_t, OP_SUM>(g, kind) : launch<int64_t, OP_NEG>(g, kind);
     }
   }
   for (void *o : owned) scratch_free(o);
@@ -532,7 +661,7 @@ static int mod_ct(int64_t as, const heal_tensor *b, const heal_tensor *r) {
            ? HEAL_OK
            : set_error(HEAL_ERR_CUDA, "mod_ct: copy failed");
   g.ap = sbuf;
-  if (!rc) rc = r->dtype == HEAL_INT32 ? launch<int32_t, OP_MOD>(g, false) : launch<int64_t, OP_MOD>(g, false);
+  if (!rc) rc = r->dtype == HEAL_INT32 ? launch<int32_t, OP_MOD>(g, KIND_GENERAL) : launch<int64_t, OP_MOD>(g, KIND_GENERAL);
   scratch_free(sbuf);
   scratch_free(owned);
   if (!rc) mark_written(r->data);

@@ -65,7 +65,10 @@ __global__ void __launch_bounds__(256) axis_modsum_kernel(const __grid_constant_
     int64_t oa = 0, orr = 0, last = 0;
     if (g.fast) {
       uint32_t rem = (uint32_t)idx;
-      for (int i = g.r.ndim - 1; i >= 0; --i) {
+#pragma unroll
+      for (int k = 0; k < HEAL_MAX_DIMS; ++k) {  // unrolled: per-axis parameters at fixed offsets
+        const int i = HEAL_MAX_DIMS - 1 - k;
+        if (i >= g.r.ndim) continue;
         const uint32_t qd = fastdiv(rem, g.fd[i]);
         const int64_t c = rem - qd * (uint32_t)g.r.dims[i];
         rem = qd;
@@ -517,31 +520,36 @@ __global__ void __launch_bounds__(256) permute_dense_kernel(const __grid_constan
 }
 
 // any strides (axes merged on the host except the two it reads); kGenU
-// elements per thread per iteration, loads issued together
+// elements per thread per iteration, loads issued together; Off is int32_t
+// when every offset of a and the result fits 32 bits
 constexpr int kGenU = 4;
 
-template <typename T>
+template <typename T, typename Off>
 __global__ void __launch_bounds__(256) permute_general_kernel(const __grid_constant__ PermuteArgs g) {
   const T *A = (const T *)g.src;
   T *R = (T *)g.out;
   const int64_t step = (int64_t)gridDim.x * blockDim.x * kGenU;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x * kGenU + threadIdx.x; base < g.n; base += step) {
-    int64_t src[kGenU], dst[kGenU];
+    Off src[kGenU], dst[kGenU];
 #pragma unroll
     for (int u = 0; u < kGenU; ++u) {
       const int64_t idx = base + (int64_t)u * blockDim.x;
-      int64_t e = 0, pm = 0, s = 0, d = 0;
+      int64_t e = 0, pm = 0;
+      Off s = 0, d = 0;
       if (idx < g.n) {
         if (g.fd.fast) {
           uint32_t rem = (uint32_t)idx;
-          for (int i = g.r.ndim - 1; i >= 0; --i) {
+#pragma unroll
+          for (int k = 0; k < HEAL_MAX_DIMS; ++k) {  // unrolled: per-axis parameters at fixed offsets
+            const int i = HEAL_MAX_DIMS - 1 - k;
+            if (i >= g.r.ndim) continue;
             const uint32_t q = fastdiv(rem, g.fd.fd[i]);
-            const int64_t c = rem - q * (uint32_t)g.r.dims[i];
+            const uint32_t c = rem - q * (uint32_t)g.r.dims[i];
             rem = q;
             if (i == g.ew) e = c;
             if (i == g.pa) pm = c;
-            else s += c * g.a.strides[i];
-            d += c * g.r.strides[i];
+            else s += (Off)c * (Off)g.a.strides[i];
+            d += (Off)c * (Off)g.r.strides[i];
           }
         } else {
           int64_t rem = idx;
@@ -550,11 +558,11 @@ __global__ void __launch_bounds__(256) permute_general_kernel(const __grid_const
             rem /= g.r.dims[i];
             if (i == g.ew) e = c;
             if (i == g.pa) pm = c;
-            else s += c * g.a.strides[i];
-            d += c * g.r.strides[i];
+            else s += (Off)(c * g.a.strides[i]);
+            d += (Off)(c * g.r.strides[i]);
           }
         }
-        s += perm_at(g, e, pm) * g.a.strides[g.pa];
+        s += (Off)perm_at(g, e, pm) * (Off)g.a.strides[g.pa];
       }
       src[u] = s;
       dst[u] = d;
@@ -633,6 +641,8 @@ static int permute(const heal_tensor *a, const heal_tensor *perms, const heal_te
         g.f_ewmod = fastdiv_make((uint32_t)l);
       }
     }
+    const int vec = 16 / elem_size(r->dtype);
+    bool gen_vec = false, off32 = false;
     if (!g.dense) {
       // general path: merge the axes other than the two whose coordinates it reads
       View *vs[2] = {&g.r, &g.a};
@@ -640,12 +650,27 @@ static int permute(const heal_tensor *a, const heal_tensor *perms, const heal_te
       coalesce_views(vs, 2, (1u << ew) | (1u << pa), map);
       g.ew = map[ew];
       g.pa = map[pa];
-      make_fast_dims(g.r, n, &g.fd);
+      // an innermost axis that is neither read axis and is contiguous in
+      // aligned 16-byte vectors in both a and the result (a ciphertext's
+      // limbs under a broadcast or transposed stack) moves as vectors: the
+      // views are rescaled to units of one vector
+      const int in = g.r.ndim - 1;
+      off32 = view_off32(g.r) && view_off32(g.a);
+      gen_vec = in != g.ew && in != g.pa && inner_vectors(g.r, vec, r->data, elem_size(r->dtype)) &&
+                inner_vectors(g.a, vec, A.data, elem_size(r->dtype));
+      if (gen_vec) {
+        for (View *v : vs) {
+          v->dims[in] /= vec;
+          for (int i = 0; i < in; ++i) v->strides[i] /= vec;
+        }
+        g.n = n / vec;
+      }
+      make_fast_dims(g.r, g.n, &g.fd);
+      off32 = off32 && g.fd.fast;
     }
     // rows of 16-byte vectors: the gathered blocks (`post` elements) are
     // whole aligned vectors and a vector never straddles two elementwise
     // coordinates; the same kernel then moves one vector per index
-    const int vec = 16 / elem_size(r->dtype);
     const bool rows = g.dense && g.fast && g.post % vec == 0 && (!g.ew_in_post || g.ew_div % vec == 0) &&
                       (uintptr_t)A.data % 16 == 0 && (uintptr_t)r->data % 16 == 0;
     if (rows) {
@@ -661,11 +686,17 @@ static int permute(const heal_tensor *a, const heal_tensor *perms, const heal_te
       else
         permute_dense_kernel<int64_t><<<grid_for(n, 256, 8), 256, 0, stream()>>>(g);
     } else {
-      const int64_t work = (n + kGenU - 1) / kGenU;
-      if (r->dtype == HEAL_INT32)
-        permute_general_kernel<int32_t><<<grid_for(work, 256, 8), 256, 0, stream()>>>(g);
-      else
-        permute_general_kernel<int64_t><<<grid_for(work, 256, 8), 256, 0, stream()>>>(g);
+      const int grid = grid_for((g.n + kGenU - 1) / kGenU, 256, 8);
+      auto go = [&](auto t_tag) {
+        typedef decltype(t_tag) TT;
+        if (off32)
+          permute_general_kernel<TT, int32_t><<<grid, 256, 0, stream()>>>(g);
+        else
+          permute_general_kernel<TT, int64_t><<<grid, 256, 0, stream()>>>(g);
+      };
+      if (gen_vec) go(uint4());
+      else if (r->dtype == HEAL_INT32) go(int32_t());
+      else go(int64_t());
     }
     rc = check_launch("permute");
   }

@@ -244,7 +244,10 @@ __global__ void __launch_bounds__(256) copy_strided_kernel(const __grid_constant
       if (idx >= a.n) continue;
       if (a.fd.fast) {
         uint32_t rem = (uint32_t)idx;
-        for (int i = a.dst.ndim - 1; i >= 0; --i) {
+#pragma unroll
+        for (int k = 0; k < HEAL_MAX_DIMS; ++k) {  // unrolled: per-axis parameters at fixed offsets
+          const int i = HEAL_MAX_DIMS - 1 - k;
+          if (i >= a.dst.ndim) continue;
           const uint32_t q = fastdiv(rem, a.fd.fd[i]);
           const int64_t c = rem - q * (uint32_t)a.dst.dims[i];
           rem = q;

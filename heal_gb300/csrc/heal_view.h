@@ -80,6 +80,32 @@ inline void coalesce_views(View *const *views, int nviews, unsigned keep, int *m
 
 // Divisions by every dim of a coordinate space, for 32-bit index
 // decomposition when its element count and dims are below 2^32.
+// True when a kernel may move `v`'s innermost axis in vectors of `vec`
+// elements of `elem` bytes from `base`: the axis is contiguous, its length is
+// a multiple of vec, and every vector starts on a vec * elem byte boundary
+// (the base aligned, every other stride a multiple of vec).
+inline bool inner_vectors(const View &v, int vec, const void *base, size_t elem) {
+  if (v.ndim < 1 || vec < 1) return false;
+  const int in = v.ndim - 1;
+  if (v.strides[in] != 1 || v.dims[in] % vec) return false;
+  if ((uintptr_t)base % ((uintptr_t)vec * elem)) return false;
+  for (int i = 0; i < in; ++i)
+    if (v.strides[i] % vec) return false;
+  return true;
+}
+
+// True when every offset of `v` fits a signed 32-bit integer: strides
+// non-negative and the largest offset below 2^31 - 1.
+inline bool view_off32(const View &v) {
+  int64_t span = 0;
+  for (int i = 0; i < v.ndim; ++i) {
+    if (v.strides[i] < 0 || v.dims[i] < 1) return false;
+    if (v.strides[i] && (v.dims[i] - 1) > (INT32_MAX - 1 - span) / v.strides[i]) return false;
+    span += (v.dims[i] - 1) * v.strides[i];
+  }
+  return span < INT32_MAX;
+}
+
 struct FastDims {
   int fast;
   FastDiv fd[HEAL_MAX_DIMS];

@@ -84,6 +84,36 @@ int main() {
     }
     ++cases;
   }
+  // inner_vectors: contiguous innermost axis, whole vectors, aligned starts
+  {
+    View a;
+    memset(&a, 0, sizeof a);
+    a.ndim = 3;
+    a.dims[0] = 4, a.dims[1] = 6, a.dims[2] = 8;
+    a.strides[0] = 48, a.strides[1] = 8, a.strides[2] = 1;
+    alignas(16) static int64_t buf[512];
+    const bool want[6] = {true, false, false, false, false, true};
+    bool got[6];
+    got[0] = inner_vectors(a, 2, buf, 8);
+    got[1] = inner_vectors(a, 2, buf + 1, 8);  // start off the 16-byte grid
+    View b = a;
+    b.strides[1] = 9;                           // a row start off the grid
+    got[2] = inner_vectors(b, 2, buf, 8);
+    b = a;
+    b.dims[2] = 7;                              // a partial vector per row
+    got[3] = inner_vectors(b, 2, buf, 8);
+    b = a;
+    b.strides[2] = 2;                           // a strided innermost axis
+    got[4] = inner_vectors(b, 2, buf, 8);
+    b = a;
+    b.strides[0] = 0;                           // broadcast outer axis
+    got[5] = inner_vectors(b, 2, buf, 8);
+    for (int i = 0; i < 6; ++i)
+      if (got[i] != want[i]) {
+        printf("inner_vectors case %d: got %d\n", i, (int)got[i]);
+        return 1;
+      }
+  }
   printf("ok %d\n", cases);
   return 0;
 }

@@ -405,3 +405,87 @@ def test_ntt_permutation_one_swap_from_bit_reversal(m):
         assert np.array_equal(ntt(x, p, pm, tw), O.ntt(x, p, pm, tw))
         y = O.ntt(x, p, pm, tw)
         assert np.array_equal(intt(y, p, pm, itw, minv), O.intt(y, p, pm, itw, minv))
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+def test_broadcast_and_strided_modops_in_vector_units(dt):
+    """Results contiguous on their innermost axis with operands contiguous or
+    broadcast there (moved 16 bytes at a time), beside the cases that must
+    stay element by element: an operand at an odd element offset, an odd
+    innermost length, a strided innermost axis."""
+    rng = np.random.default_rng(7 if dt == np.int32 else 8)
+    hi = 2 ** 30 if dt == np.int32 else 2 ** 62
+    L, N = 16, 256
+    qs = np.array(P.ntt_primes(hi, 8, L), dt)
+    lo = int(qs.min())
+    ct = rng.integers(0, lo, size=(2, N, 1, L)).astype(dt)
+    pt = rng.integers(0, lo, size=(N, 1, L)).astype(dt)
+    for f, o in [("heal_modmul_ttt", O.modmul), ("heal_modsum_ttt", O.modsum)]:
+        # plaintext broadcast over the two polynomials, and the reverse roles
+        assert np.array_equal(run(f, ct, pt, qs, out_shape=ct.shape, dtype=dt), o(ct, pt, qs, out_shape=ct.shape)), f
+        assert np.array_equal(run(f, pt, ct, qs, out_shape=ct.shape, dtype=dt), o(pt, ct, qs, out_shape=ct.shape)), f
+    # a stack of rotations times its diagonals: [d, 2, N/d, d, L] x [d, 1, 1, d, L]
+    d = 4
+    stack = rng.integers(0, lo, size=(d, 2, N // d, d, L)).astype(dt)
+    diag = rng.integers(0, lo, size=(d, 1, 1, d, L)).astype(dt)
+    want = O.modmul(stack, diag, qs, out_shape=stack.shape)
+    assert np.array_equal(run("heal_modmul_ttt", stack, diag, qs, out_shape=stack.shape, dtype=dt), want)
+    ds = up(stack)  # in place, as the three-call product runs
+    capi.call("heal_modmul_ttt", ds, up(diag), up(qs), ds)
+    assert np.array_equal(ds.numpy(), want)
+    # a transposed operand (outer axes swapped, limbs still contiguous), a scalar b, negation
+    x = rng.integers(-hi, hi, size=(N, 2, L)).astype(dt)
+    xt = up(x).moveaxis(1, 0)
+    xn = np.ascontiguousarray(np.moveaxis(x, 1, 0))
+    assert np.array_equal(run("heal_modmul_ttt", xt, up(ct.reshape(2, N, L)), up(qs), out_shape=(2, N, L), dtype=dt),
+                          O.modmul(xn, ct.reshape(2, N, L), qs))
+    assert np.array_equal(run("heal_modmul_tct", xt, 12345, up(qs), out_shape=(2, N, L), dtype=dt),
+                          O.modmul(xn, 12345, qs))
+    assert np.array_equal(run("heal_modneg_tt", xt, up(qs), out_shape=(2, N, L), dtype=dt), O.modneg(xn, qs))
+    den = rng.integers(1, 1000, size=(2, N, L)).astype(dt)
+    assert np.array_equal(run("heal_mod_tt", xt, up(den), out_shape=(2, N, L), dtype=dt), O.mod(xn, den))
+    # moduli per row and limb ([N, L] broadcast over the polynomials), and one modulus broadcast along the limbs
+    prow = rng.integers(lo // 2, lo, size=(N, 1, L)).astype(dt)
+    assert np.array_equal(run("heal_modmul_ttt", ct, pt, prow, out_shape=ct.shape, dtype=dt),
+                          O.modmul(ct, pt, prow, out_shape=ct.shape))
+    p1 = qs[:1].copy()
+    assert np.array_equal(run("heal_modsum_ttt", ct, pt, p1, out_shape=ct.shape, dtype=dt),
+                          O.modsum(ct, pt, p1, out_shape=ct.shape))
+    # one element off the 16-byte grid: the element-wise kernel
+    buf = up(np.concatenate([np.zeros(1, dt), pt.ravel()]))
+    off = capi.DeviceArray(buf.buf, dt, (N, 1, L), None, np.dtype(dt).itemsize)
+    assert np.array_equal(run("heal_modmul_ttt", up(ct), off, up(qs), out_shape=ct.shape, dtype=dt),
+                          O.modmul(ct, pt, qs, out_shape=ct.shape))
+    # an odd number of limbs, and limbs taken every other element
+    q3 = qs[:3].copy()
+    c3 = np.ascontiguousarray(ct[..., :3])
+    p3 = np.ascontiguousarray(pt[..., :3])
+    assert np.array_equal(run("heal_modmul_ttt", c3, p3, q3, out_shape=c3.shape, dtype=dt),
+                          O.modmul(c3, p3, q3, out_shape=c3.shape))
+    wide = up(np.repeat(pt, 2, axis=2))
+    half = capi.DeviceArray(wide.buf, dt, (N, 1, L), (2 * L, 2 * L, 2))
+    assert np.array_equal(run("heal_modmul_ttt", up(ct), half, up(qs), out_shape=ct.shape, dtype=dt),
+                          O.modmul(ct, pt, qs, out_shape=ct.shape))
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+def test_permute_strided_sources_in_vector_units(dt):
+    """A ciphertext expanded over a stack of rotations (stride 0 on the
+    elementwise axis) and a transposed source: limbs move 16 bytes at a time.
+    An odd element offset stays element by element."""
+    rng = np.random.default_rng(11)
+    d, N, L = 8, 512, 16
+    ct = rng.integers(-1000, 1 << 30, size=(2, N, L)).astype(dt)
+    perms = np.stack([rng.permutation(N) for _ in range(d)]).astype(dt)
+    src = up(ct).reshape((1, 2, N, L)).expand(0, d)
+    want = O.permute(np.ascontiguousarray(np.broadcast_to(ct[None], (d, 2, N, L))), perms, 0, 2)
+    assert np.array_equal(run("heal_permute", src, up(perms), 0, 2, out_shape=(d, 2, N, L), dtype=dt), want)
+    x = rng.integers(0, 1 << 30, size=(N, 2, L)).astype(dt)
+    p2 = np.stack([rng.permutation(N) for _ in range(2)]).astype(dt)
+    xt = up(x).moveaxis(1, 0)
+    assert np.array_equal(run("heal_permute", xt, up(p2), 0, 1, out_shape=(2, N, L), dtype=dt),
+                          O.permute(np.ascontiguousarray(np.moveaxis(x, 1, 0)), p2, 0, 1))
+    buf = up(np.concatenate([np.zeros(1, dt), x.ravel()]))
+    off = capi.DeviceArray(buf.buf, dt, (N, 2, L), None, np.dtype(dt).itemsize).moveaxis(1, 0)
+    assert np.array_equal(run("heal_permute", off, up(p2), 0, 1, out_shape=(2, N, L), dtype=dt),
+                          O.permute(np.ascontiguousarray(np.moveaxis(x, 1, 0)), p2, 0, 1))
