@@ -86,7 +86,8 @@ int mod_table(const heal_tensor &p, ModTable *out);
 // Moduli summary of a [k] tensor (first use synchronises once).
 struct ModInfo {
   int64_t min_q, max_q;
-  const int64_t *q;  // device, [k] int64 copy of the moduli
+  const int64_t *q;        // device, [k] int64 copy of the moduli
+  const uint64_t *qone;    // device, [k] floor(2^64 / q) (2^64 - 1 for q = 1)
 };
 int mod_info(const heal_tensor &p, ModInfo *out);
 

@@ -170,6 +170,14 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
                    : mi.max_q < (int64_t(1) << 31) ? MODE_N32
                                                    : MODE_W64_LAZY;
   const bool wide = mode == MODE_W64_LAZY;
+  // 64-bit growing ranges where the headroom allows (heal_ntt_kernels.cuh):
+  // forward values stay below (1 + 2 log2 m) q <= 49q < 2^63; an inverse pass
+  // of P stages ends below 2^P q < 2^63
+  auto mode_of = [&](int pbits) {
+    if (!wide) return mode;
+    const int lim = inv ? 63 - pbits : 57;
+    return mi.max_q < (int64_t(1) << lim) ? (int)MODE_W64_GROW : mode;
+  };
   PermInfo pi;
   HEAL_CHECK(perm_info(*perm, &pi));
   if (pi.bad) return set_error(HEAL_ERR_OUT_OF_RANGE, "Index out of bounds.");
@@ -194,6 +202,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   base.tw_s0 = tw->strides[0];
   base.tw_s1 = tw->strides[1];
   base.q = mi.q;
+  base.qone = mi.qone;
   base.bitrev = pi.bitrev_log;  // every table this call indexes is the bit reversal (its own inverse)
   if (inv) {
     base.minv_pairs = mt.pairs;
@@ -246,7 +255,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
     } else {
       x.store_gather = pi.perm32;
     }
-    rc = launch_any(x, nb, is32, mode, inv);
+    rc = launch_any(x, nb, is32, mode_of(logm), inv);
   } else {
     // two passes through a dense [l, m, r, k] scratch tensor
     const int p1 = plan.first_log, p2 = logm - p1;
@@ -266,24 +275,29 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
       x.dst = T1.data;
       set_strides(x.ds, T1);
       x.canon_load = 1;
-      rc = launch_any(x, nb, is32, mode, false);
+      // growing ranges carry across the two passes when both run them and the
+      // second runs the register kernel (at least 3 stages)
+      const int m1 = mode_of(p1), m2 = mode_of(p2);
+      x.lazy_out = m1 == MODE_W64_GROW && m2 == MODE_W64_GROW && p2 >= 3;
+      rc = launch_any(x, nb, is32, m1, false);
       if (!rc) {
         NttArgs y = base;  // pass 2: remaining stages on contiguous blocks
         nb = cfg(y, p2, KIND_BLOCK);
         y.src = T1.data;
         set_strides(y.ss, T1);
+        y.unreduced_in = x.lazy_out;
         if (pi.bijective) {
           y.dst = res->data;
           set_strides(y.ds, *res);
           y.store_scatter = pi.inv32;
-          rc = launch_any(y, nb, is32, mode, false);
+          rc = launch_any(y, nb, is32, m2, false);
         } else {
           heal_tensor T2 = T1;
           rc = scratch_alloc((size_t)s * elem_size(dt), &tmp2);
           T2.data = tmp2;
           y.dst = T2.data;
           set_strides(y.ds, T2);
-          if (!rc) rc = launch_any(y, nb, is32, mode, false);
+          if (!rc) rc = launch_any(y, nb, is32, m2, false);
           if (!rc) {
             int64_t n = l * m * r * k;
             int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 16);
@@ -312,7 +326,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
       x.dst = T1.data;
       set_strides(x.ds, T1);
       x.canon_load = 1;
-      rc = launch_any(x, nb, is32, mode, true);
+      rc = launch_any(x, nb, is32, mode_of(p1), true);
       if (!rc) {
         NttArgs y = base;  // pass 2: remaining stages on strided sets, then m_inv
         nb = cfg(y, p2, KIND_STRIDED);
@@ -321,7 +335,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
         y.dst = res->data;
         set_strides(y.ds, *res);
         y.scale = 1;
-        rc = launch_any(y, nb, is32, mode, true);
+        rc = launch_any(y, nb, is32, mode_of(p2), true);
       }
     }
   }

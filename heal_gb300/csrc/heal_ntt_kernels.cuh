@@ -50,6 +50,9 @@ struct NttArgs {
   const void *tw_raw;
   int64_t tw_s0, tw_s1;
   const int64_t *q;
+  const uint64_t *qone;  // floor(2^64 / q) per limb: Shoup companion of 1 (growing-range reduction)
+  int lazy_out;          // growing ranges, forward first pass: store unreduced values (below 2^63)
+  int unreduced_in;      // the input is such a first pass's output (non-negative, possibly >= q)
   const void *minv_pairs;
   const int *minv_neg;
   const void *minv_raw;
@@ -83,10 +86,23 @@ struct Word<false> {
 //   0  32-bit words, canonical values     (every q < 2^31)
 //   1  32-bit words, Harvey's lazy ranges (every q < 2^30: 4q < 2^32)
 //   2  64-bit words, Harvey's lazy ranges (every q < 2^62: 4q < 2^64)
+//   3  64-bit words, growing ranges       (q < 2^57 forward, q < 2^(63 - P) inverse)
 // Lazy butterflies keep forward values in [0, 4q) and inverse values in
 // [0, 2q) with one conditional subtraction per butterfly instead of three;
 // every pass still ends on canonical residues.
-enum { MODE_N32 = 0, MODE_N32_LAZY = 1, MODE_W64_LAZY = 2 };
+// Growing ranges drop that subtraction too, using the headroom of 64-bit
+// words over the modulus.  Forward (Cooley-Tukey): with u < Bq and the Shoup
+// product t in [0, 2q), u + t and u - t + 2q both lie in [0, (B + 2)q), so a
+// canonical input is below (1 + 2s)q after s stages and below 49q after the
+// 24 stages of the longest transform.  A first pass hands its unreduced
+// values to the second (`lazy_out`); the last pass reduces once per point
+// with a Shoup product by 1 (companion floor(2^64 / q)).  Inverse
+// (Gentleman-Sande): the sum of two values below 2^s q is below 2^(s+1) q and
+// a - b + 2^s q is non-negative, so stage s adds the constant q << s; the
+// product goes back to [0, 2q); a pass of P stages ends below 2^P q and
+// reduces once per point (the m^-1 product does it on the last pass).
+enum { MODE_N32 = 0, MODE_N32_LAZY = 1, MODE_W64_LAZY = 2, MODE_W64_GROW = 3 };
+__host__ __device__ constexpr bool mode_wide(int mode) { return mode >= MODE_W64_LAZY; }
 
 // log2 of the points one thread of the register kernel holds (a radix-2^lpt
 // step per shared-memory exchange): 16 points for the forward transform in
@@ -366,10 +382,11 @@ __device__ __forceinline__ int point_of(int step, int r, int e) {
 // One register step: stages [kLPT*STEP, kLPT*STEP + qn) on the kPT >> qn
 // sets of 2^qn points this thread holds.
 template <int MODE, bool INV, int LOGP, int STEP>
-__device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W (&v)[1 << lpt_of(MODE, INV)], int r, int64_t G,
-                                         const typename Word<MODE == MODE_W64_LAZY>::Pair *twp,
-                                         typename Word<MODE == MODE_W64_LAZY>::W q) {
-  constexpr bool WIDE = MODE == MODE_W64_LAZY;
+__device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[1 << lpt_of(MODE, INV)], int r, int64_t G,
+                                         const typename Word<mode_wide(MODE)>::Pair *twp,
+                                         typename Word<mode_wide(MODE)>::W q) {
+  constexpr bool WIDE = mode_wide(MODE);
+  constexpr bool GROW = MODE == MODE_W64_GROW;
   constexpr bool LAZY = MODE != MODE_N32;
   constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
   typedef typename Word<WIDE>::W W;
@@ -395,7 +412,12 @@ __device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
             const int a = base + gl * 2 * dist + off, b = a + dist;
-            if (LAZY) {
+            if (GROW) {
+              const W u = v[a];
+              const W tv = mulw_lazy<WIDE>(v[b], pr, q);
+              v[a] = u + tv;
+              v[b] = u - tv + q2;
+            } else if (LAZY) {
               W u = v[a];
               u = u >= q2 ? u - q2 : u;
               const W tv = mulw_lazy<WIDE>(v[b], pr, q);
@@ -414,13 +436,18 @@ __device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W
       } else {
         const int hi = id >> st0;
         const int dist = 1 << kk;
+        const W qs = q << st;  // growing ranges: every value entering stage st is below 2^st q
 #pragma unroll
         for (int gl = 0; gl < (1 << (qn - 1 - kk)); ++gl) {
           const Pair pr = __ldg(twp + G * (int64_t)(P >> (st + 1)) + ((int64_t)hi << (qn - 1 - kk)) + gl);
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
             const int a = base + gl * 2 * dist + off, b = a + dist;
-            if (LAZY) {
+            if (GROW) {
+              const W d = v[a] - v[b] + qs;
+              v[a] = v[a] + v[b];
+              v[b] = mulw_lazy<WIDE>(d, pr, q);
+            } else if (LAZY) {
               W s = v[a] + v[b];
               s = s >= q2 ? s - q2 : s;
               const W d = v[a] - v[b] + q2;
@@ -442,11 +469,11 @@ __device__ __forceinline__ void reg_step(typename Word<MODE == MODE_W64_LAZY>::W
 
 // Steps STEP .. NSTEP-1, exchanging through the shared tile between steps.
 template <int MODE, bool INV, int LOGP, int STEP>
-__device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::W (&v)[1 << lpt_of(MODE, INV)], int r, int c, int logC,
+__device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)[1 << lpt_of(MODE, INV)], int r, int c, int logC,
                                           int64_t *tile, int64_t G,
-                                          const typename Word<MODE == MODE_W64_LAZY>::Pair *twp,
-                                          typename Word<MODE == MODE_W64_LAZY>::W q) {
-  typedef typename Word<MODE == MODE_W64_LAZY>::W W;
+                                          const typename Word<mode_wide(MODE)>::Pair *twp,
+                                          typename Word<mode_wide(MODE)>::W q) {
+  typedef typename Word<mode_wide(MODE)>::W W;
   constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
   constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
   if constexpr (STEP < NSTEP) {
@@ -474,7 +501,7 @@ __device__ __forceinline__ void reg_steps(typename Word<MODE == MODE_W64_LAZY>::
 #endif
 template <typename T, int MODE, bool INV, int LOGP>
 __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
-  constexpr bool WIDE = MODE == MODE_W64_LAZY;
+  constexpr bool WIDE = mode_wide(MODE);
   constexpr bool LAZY = MODE != MODE_N32;
   constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
   typedef typename Word<WIDE>::W W;
@@ -516,8 +543,14 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
   const bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
                      (g.scale && g.minv_neg && *g.minv_neg);
   if (exact) {
+    // a growing-range first pass left its fast tiles' values unreduced; the
+    // reference's arithmetic sees canonical residues there
 #pragma unroll
-    for (int e = 0; e < kPT; ++e) tile[tidx(point_of<INV, LOGP, kLPT>(0, r, e), c, logC)] = raw[e];
+    for (int e = 0; e < kPT; ++e) {
+      int64_t w = raw[e];
+      if (g.unreduced_in && w >= q64) w %= q64;
+      tile[tidx(point_of<INV, LOGP, kLPT>(0, r, e), c, logC)] = w;
+    }
     __syncthreads();
     exact_tile<T, INV>(g, x, tile);
     return;
@@ -534,8 +567,19 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
   }
   reg_steps<MODE, INV, LOGP, 0>(v, r, c, logC, tile, x.G, twp, q);
 
-  // ---- back to canonical residues (forward values < 4q, inverse < 2q)
-  if (LAZY) {
+  // ---- back to canonical residues (forward values < 4q, inverse < 2q;
+  // growing ranges: a Shoup product by 1, unless the m^-1 product follows or
+  // the next pass takes the values as they are)
+  if (MODE == MODE_W64_GROW) {
+    if (INV ? !g.scale : !g.lazy_out) {
+      const W one = (W)g.qone[tq];
+#pragma unroll
+      for (int e = 0; e < kPT; ++e) {
+        const W u = v[e] - (W)mulhi64((uint64_t)v[e], (uint64_t)one) * q;
+        v[e] = u >= q ? u - q : u;
+      }
+    }
+  } else if (LAZY) {
 #pragma unroll
     for (int e = 0; e < kPT; ++e) {
       W u = v[e];

@@ -38,7 +38,7 @@ static int launch_typed(const NttArgs &a, int64_t nblocks) {
   switch (a.p) {
     case 3:
       if constexpr (lpt_of(MODE, INV) <= 3) return launch_reg<T, MODE, INV, 3>(a, nblocks);
-      return launch_small<T, MODE == MODE_W64_LAZY, INV>(a, nblocks);
+      return launch_small<T, mode_wide(MODE), INV>(a, nblocks);
     case 4: return launch_reg<T, MODE, INV, 4>(a, nblocks);
     case 5: return launch_reg<T, MODE, INV, 5>(a, nblocks);
     case 6: return launch_reg<T, MODE, INV, 6>(a, nblocks);
@@ -48,7 +48,7 @@ static int launch_typed(const NttArgs &a, int64_t nblocks) {
     case 10: return launch_reg<T, MODE, INV, 10>(a, nblocks);
     case 11: return launch_reg<T, MODE, INV, 11>(a, nblocks);
     case 12: return launch_reg<T, MODE, INV, 12>(a, nblocks);
-    default: return launch_small<T, MODE == MODE_W64_LAZY, INV>(a, nblocks);
+    default: return launch_small<T, mode_wide(MODE), INV>(a, nblocks);
   }
 }
 
@@ -56,6 +56,7 @@ static int launch_typed(const NttArgs &a, int64_t nblocks) {
 template <typename T, bool INV>
 static int launch_direction_typed(const NttArgs &a, int64_t nblocks, int mode) {
   if constexpr (sizeof(T) == 8) {
+    if (mode == MODE_W64_GROW) return launch_typed<T, MODE_W64_GROW, INV>(a, nblocks);
     if (mode == MODE_W64_LAZY) return launch_typed<T, MODE_W64_LAZY, INV>(a, nblocks);
   }
   if (mode == MODE_N32_LAZY) return launch_typed<T, MODE_N32_LAZY, INV>(a, nblocks);

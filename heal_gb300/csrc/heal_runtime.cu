@@ -527,10 +527,13 @@ struct MinMax {
 __device__ __forceinline__ unsigned long long enc64(int64_t x) { return (unsigned long long)x ^ 0x8000000000000000ull; }
 static int64_t dec64(unsigned long long x) { return (int64_t)(x ^ 0x8000000000000000ull); }
 
-__global__ void mod_info_kernel(const void *p, int dtype, int64_t stride, int64_t k, int64_t *q, MinMax *mm) {
+__global__ void mod_info_kernel(const void *p, int dtype, int64_t stride, int64_t k, int64_t *q, uint64_t *qone,
+                                MinMax *mm) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
     int64_t v = load_any(p, dtype, i * stride);
     q[i] = v;
+    // floor(2^64 / q); 2^64 - 1 stands in for q = 1 (the Shoup bound still holds)
+    qone[i] = v > 1 ? (uint64_t)((((u128)1) << 64) / (u128)(uint64_t)v) : ~0ull;
     atomicMin(&mm->min_enc, enc64(v));
     atomicMax(&mm->max_enc, enc64(v));
   }
@@ -545,14 +548,14 @@ int mod_info(const heal_tensor &p, ModInfo *out) {
     CacheEntry &n = cache_insert(key, {p.data});
     int64_t k = p.ndim ? p.dims[0] : 1;
     void *buf, *mmb;
-    HEAL_CHECK(scratch_alloc(sizeof(int64_t) * std::max<int64_t>(k, 1), &buf));
+    HEAL_CHECK(scratch_alloc(2 * sizeof(int64_t) * std::max<int64_t>(k, 1), &buf));  // q, then floor(2^64 / q)
     n.bufs.push_back(buf);
     HEAL_CHECK(scratch_alloc(sizeof(MinMax), &mmb));
     MinMax init = {~0ull, 0ull};
     HEAL_TRY_CUDA(cudaMemcpyAsync(mmb, &init, sizeof init, cudaMemcpyHostToDevice, stream()));
     if (k) {
       mod_info_kernel<<<grid_for(k, 128), 128, 0, stream()>>>(p.data, p.dtype, p.ndim ? p.strides[0] : 0, k,
-                                                              (int64_t *)buf, (MinMax *)mmb);
+                                                              (int64_t *)buf, (uint64_t *)buf + k, (MinMax *)mmb);
       HEAL_CHECK(check_launch("mod_info"));
     }
     MinMax h;
@@ -567,6 +570,7 @@ int mod_info(const heal_tensor &p, ModInfo *out) {
   out->min_q = e->i0;
   out->max_q = e->i1;
   out->q = (const int64_t *)e->bufs[0];
+  out->qone = (const uint64_t *)e->bufs[0] + std::max<int64_t>(p.ndim ? p.dims[0] : 1, 1);
   return HEAL_OK;
 }
 

@@ -489,3 +489,56 @@ def test_permute_strided_sources_in_vector_units(dt):
     off = capi.DeviceArray(buf.buf, dt, (N, 2, L), None, np.dtype(dt).itemsize).moveaxis(1, 0)
     assert np.array_equal(run("heal_permute", off, up(p2), 0, 1, out_shape=(2, N, L), dtype=dt),
                           O.permute(np.ascontiguousarray(np.moveaxis(x, 1, 0)), p2, 0, 1))
+
+
+# ------------------------------------------- 64-bit growing-range boundaries
+# The 64-bit transforms skip per-butterfly reductions while the modulus leaves
+# headroom: forward for q < 2^57 (values stay below 49q), an inverse pass of P
+# stages for q < 2^(63 - P).  Primes just below and just above each threshold,
+# with pass splits that move the inverse's pass lengths across them.
+GROW_CASES = [
+    # (m, prime bound, first-pass log2 per call: 0 = one pass)
+    (1 << 16, 2**57, (8, 4, 12)),    # forward grows to 33q; inverse passes: lazy ranges
+    (1 << 16, 2**55, (8, 4, 12)),    # 8-stage inverse passes grow; 12-stage ones do not
+    (1 << 16, 2**51, (8, 4, 12)),    # every pass grows
+    (4096, 2**51, (0, 6)),           # one 12-stage pass at its inverse threshold
+    (4096, 2**52, (0, 6)),
+    (1 << 20, 2**57, (10, 8)),       # the forward's longest tested chain: 41q
+]
+
+
+@pytest.mark.parametrize("m,bound,splits", GROW_CASES)
+def test_ntt_growing_range_thresholds(m, bound, splits):
+    k = 2
+    qs = P.ntt_primes(bound, m, k)
+    qs[1] = P.ntt_primes(2**40, m, 1)[0]        # mixed widths: the largest modulus picks the mode
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m)
+    a = P.residues(m ^ bound.bit_length(), (1, m, 1, k), qs)
+    want = O.ntt(a, p, perm, tw)
+    code = capi.DTYPES[np.dtype(np.int64)]
+    dx, dp, dperm, dtw, ditw, dminv, dwant = (up(v) for v in (a, p, perm, tw, itw, minv, want))
+    out = capi.DeviceArray.empty(a.shape, np.int64)
+    try:
+        for s in splits:
+            for inv in (0, 1):
+                capi.check(capi.lib().heal_ntt_set_plan(code, inv, m, k, 4, s))
+            capi.call("heal_ntt", dx, dp, dperm, dtw, None, None, out)
+            assert np.array_equal(out.numpy(), want), s
+            capi.call("heal_intt", dwant, dp, dperm, ditw, dminv, None, None, out)
+            assert np.array_equal(out.numpy(), a), s
+    finally:
+        capi.check(capi.lib().heal_ntt_clear_plans())
+
+
+@pytest.mark.parametrize("m", [8192, 1 << 16])
+def test_two_pass_negative_values_beside_unreduced_tiles(m):
+    # a few negative inputs send some first-pass tiles to the reference's
+    # arithmetic while their neighbours hand unreduced values to the second pass
+    qs = P.ntt_primes(2**50, m, 3)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m)
+    a = P.residues(21, (2, m, 1, 3), qs)
+    a[0, 5, 0, 1] = -7
+    a[1, m // 2 + 3, 0, 2] = -(2**45)
+    a[1, 17, 0, 0] = 2**55                      # non-negative, above q: reduced on load
+    assert np.array_equal(ntt(a, p, perm, tw), O.ntt(a, p, perm, tw))
+    assert np.array_equal(intt(a, p, perm, itw, minv), O.intt(a, p, perm, itw, minv, exact=1))
