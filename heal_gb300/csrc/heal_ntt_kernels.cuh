@@ -145,7 +145,8 @@ __device__ __forceinline__ const Pair *tw_row(const NttArgs &g, int64_t t) {
 }
 
 // shared-tile word index of point s, column c
-__device__ __forceinline__ int tidx(int s, int c, int logC) { return ((s ^ ((s >> 4) & 15)) << logC) + c; }
+__host__ __device__ constexpr int swz_of(int s) { return s ^ ((s >> 4) & 15); }
+__device__ __forceinline__ int tidx(int s, int c, int logC) { return (swz_of(s) << logC) + c; }
 
 struct TileCtx {
   int64_t rset, i, j, t0, G;
@@ -479,13 +480,23 @@ __device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)
   if constexpr (STEP < NSTEP) {
     if constexpr (STEP > 0) {
       // the fast path exchanges words of its own width (4 bytes in the
-      // 32-bit modes); the exact path never shares a CTA with it
+      // 32-bit modes); the exact path never shares a CTA with it.
+      // Addresses: a thread's points in a step are point_of(step, r, 0) | B(e)
+      // with disjoint bits, B linear in the bits of e, and the swizzle is
+      // linear over XOR, so tidx(point, c) = tidx(point_of(step, r, 0), c) ^
+      // (swz(B(e)) << logC): one per-thread base and a constant per point.
       W *wt = reinterpret_cast<W *>(tile);
+      {
+        const int ia = tidx(point_of<INV, LOGP, kLPT>(STEP - 1, r, 0), c, logC);
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) wt[tidx(point_of<INV, LOGP, kLPT>(STEP - 1, r, e), c, logC)] = v[e];
+        for (int e = 0; e < kPT; ++e) wt[ia ^ (swz_of(point_of<INV, LOGP, kLPT>(STEP - 1, 0, e)) << logC)] = v[e];
+      }
       __syncthreads();
+      {
+        const int ia = tidx(point_of<INV, LOGP, kLPT>(STEP, r, 0), c, logC);
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) v[e] = wt[tidx(point_of<INV, LOGP, kLPT>(STEP, r, e), c, logC)];
+        for (int e = 0; e < kPT; ++e) v[e] = wt[ia ^ (swz_of(point_of<INV, LOGP, kLPT>(STEP, 0, e)) << logC)];
+      }
       __syncthreads();
     }
     reg_step<MODE, INV, LOGP, STEP>(v, r, G, twp, q);
