@@ -341,6 +341,41 @@ def our_arm(args):
     ms_one, _ = timed(chain_step, args.steps)
     value_one = whole_job_rate(args.steps, world, ms_one)
 
+    # ---- the same chain with its tail fused: modmul, axis_modsum and permute
+    # as one heal_modmul_axis_sum_permute call (4 HEAL calls per step)
+    want0 = outs[0].numpy()
+
+    def fused_step2(s):
+        if s % 2:
+            on(side)
+            ch2.run_fused(cts[s % RING], outs[s % RING])
+            on(None)
+        else:
+            ch.run_fused(cts[s % RING], outs[s % RING])
+
+    fused_step = lambda s: ch.run_fused(cts[s % RING], outs[s % RING])
+    for w in range(args.warmup):
+        fused_step2(w)
+    ms_f2, launches_f = timed2(fused_step2, args.steps)
+    for w in range(args.warmup):
+        fused_step(w)
+    ms_f1, _ = timed(fused_step, args.steps)
+    ch.run_fused(cts[0], outs[0])
+    assert np.array_equal(outs[0].numpy(), want0), "fused chain differs from the per-call chain"
+    tail = lambda s: capi.call("heal_modmul_axis_sum_permute", ch.prod_moved, ch.key_moved, ch.dev["p"], 3,
+                               ch.dev["gal"], 2, 1, outs[s % RING])
+    for w in range(3):
+        tail(w)
+    tail_ms, _ = timed(tail, args.steps)
+    value_f = whole_job_rate(args.steps, world, ms_f2)
+    fused_chain = {"value": value_f, "unit": "chains/s", "value_one_stream": whole_job_rate(args.steps, world, ms_f1),
+                   "vs_per_call": value_f / value, "calls_per_step": 4, "launches_per_step": launches_f / args.steps,
+                   "tail_ms_per_call": tail_ms / args.steps,
+                   "tail_achieved_GBps": (2 * 2 * N * L * D + 2 * N * L) * 8 / (tail_ms / args.steps / 1e3) / 1e9,
+                   "hbm_frac": ch.bytes_per_chain_fused() * value_f / world / 1e9 / peaks()[0],
+                   "workload": "the same chain; modmul(key) -> axis_modsum(digits) -> permute as one "
+                               "heal_modmul_axis_sum_permute call; bit-identical to the per-call chain (checked)"}
+
     # ---- batched NTT of the digits (the dominant kernel) and the per-call split
     ntt_step = lambda s: capi.call("heal_ntt", ch.dig_flat, ch.dev["p_t"], ch.dev["perm"], ch.dev["tw_t"],
                                    None, None, ch.dn)
@@ -481,7 +516,7 @@ def our_arm(args):
                                     "compute streams",
                         "serial_value": e2e_serial},
                 "gpu_launches": launches, "launches_per_step": launches / args.steps,
-                "split_ms": split_ms, "ntt_plans": plans,
+                "split_ms": split_ms, "ntt_plans": plans, "fused_chain": fused_chain,
                 "clocks": clocks, "cpu_baseline": cpu, "configs": configs}
         print(json.dumps(line), flush=True)
     if world > 1:

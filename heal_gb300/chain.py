@@ -10,6 +10,7 @@ the 2 ciphertext components as l and the L RNS limbs as k):
   acc   = axis_modsum(prod viewed [2, N, 1, D, L], p, axis=3)
   out   = permute(acc, galois[1, N], elementwise_axis=2, perm_axis=1)
 
+(run_fused replaces the last three calls with one heal_modmul_axis_sum_permute.)
 Every step is one C-ABI call (include/heal_gb300.h); the reshape and the
 digit-axis move are stride-only views.  The moduli are the L largest primes
 q < 2^bound_bits with q = 1 (mod 2N); the key is seeded uniform residues; the
@@ -46,6 +47,7 @@ class KeyswitchChain:
         self.acc = E((2, n, 1, limbs), self.dtype, zero=False)
         self.dig_flat = self.dig.reshape((2, n, 1, limbs * digits))
         self.prod_moved = self.dn.reshape((2, n, 1, limbs, digits)).moveaxis(4, 3)
+        self.key_moved = self.dev["key"].reshape((2, n, 1, limbs, digits)).moveaxis(4, 3)
 
     def shape(self):
         return (2, self.n, 1, self.L)
@@ -86,6 +88,25 @@ class KeyswitchChain:
         capi.call("heal_modmul_ttt", self.dn, d["key"], d["p_t"], self.dn)
         capi.call("heal_axis_modsum", self.prod_moved, d["p"], self.acc, 3)
         capi.call("heal_permute", self.acc, d["gal"], out, 2, 1)
+
+    def run_fused(self, ct: capi.DeviceArray, out: capi.DeviceArray):
+        """The same step with its tail fused: modmul, axis_modsum and permute
+        as one heal_modmul_axis_sum_permute call on the NTT digits and the key
+        (bit-identical to run(); the product and the digit sum are never
+        written).  4 HEAL calls."""
+        d = self.dev
+        capi.call("heal_intt", ct, d["p"], d["perm"], d["itw"], d["minv"], None, None, self.x)
+        capi.call("heal_g_decomposition", self.x, self.dig, self.D, self.bits)
+        capi.call("heal_ntt", self.dig_flat, d["p_t"], d["perm"], d["tw_t"], None, None, self.dn)
+        capi.call("heal_modmul_axis_sum_permute", self.prod_moved, self.key_moved, d["p"], 3, d["gal"], 2, 1, out)
+
+    def bytes_per_chain_fused(self) -> int:
+        """Algorithmic bytes of run_fused: the first three calls as in run(),
+        then one read of the digits and the key and one write of the result."""
+        e = self.dtype.itemsize
+        ct = 2 * self.n * self.L * e
+        dg = ct * self.D
+        return (2 * ct) + (ct + dg) + (2 * dg) + (2 * dg + ct)
 
     # ---- algorithmic bytes (reads + writes of the six calls, tables excluded)
     def bytes_per_chain(self) -> int:

@@ -41,7 +41,9 @@ struct FusedArgs {
   int last;               // last axis in result coordinates
   int64_t a_pa;           // a's stride along the (innermost) gathered axis
   int64_t ps0, ps1;       // perms strides: reduced axis, flattened gathered index
-  int gather32;           // every gathered offset index * a_pa fits in 31 bits
+  int gather32;           // every gathered offset index * a_pa (and * b_pa) fits in 31 bits
+  int prow;               // POST: result axis whose coordinate selects the perms row
+  int64_t b_pa;           // POST: b's stride along the gathered axis
   const void *a, *b, *perms;
   int perms_dtype;
   const void *ptab;       // MG64 / MG32 per modulus
@@ -85,7 +87,10 @@ __device__ __forceinline__ int64_t exact_step(int64_t sum, int64_t a, int64_t b,
 #endif
 constexpr int kFusedU = HEAL_FUSED_U;
 
-template <typename T, typename PT, typename Off>
+// POST = false: a' gathered with perms row = the reduced index (modmul_axis_sum);
+// POST = true: a and b both gathered with one perms row per result element,
+// selected by its coordinate along g.prow (permute after the reduction).
+template <typename T, typename PT, typename Off, bool POST>
 __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_constant__ FusedArgs g) {
   typedef typename FusedMG<T>::type M;
   const T *A = (const T *)g.a;
@@ -95,7 +100,7 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
   const Off a_ax = (Off)g.a_ax, b_ax = (Off)g.b_ax, ps0 = (Off)g.ps0;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t a0 = 0, b0 = 0, r0 = 0, t = 0, cp = 0, cp2 = 0;
+    int64_t a0 = 0, b0 = 0, r0 = 0, t = 0, cp = 0, cp2 = 0, cr = 0;
     if (g.fd.fast) {
       uint32_t rem = (uint32_t)idx;
 #pragma unroll
@@ -108,6 +113,7 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
         if (i == g.last) t = c;
         if (i == g.pa) cp = c;
         if (i == g.pa2) cp2 = c;
+        if (POST && i == g.prow) cr = c;
         a0 += c * g.ao.strides[i];
         b0 += c * g.bo.strides[i];
         r0 += c * g.r.strides[i];
@@ -120,6 +126,7 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
         if (i == g.last) t = c;
         if (i == g.pa) cp = c;
         if (i == g.pa2) cp2 = c;
+        if (POST && i == g.prow) cr = c;
         a0 += c * g.ao.strides[i];
         b0 += c * g.bo.strides[i];
         r0 += c * g.r.strides[i];
@@ -163,20 +170,25 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
     // indices of the next batch are fetched while this batch's operands load
     Off ai = (Off)a0, bi = (Off)b0, pi = perm ? (Off)(cp * g.ps1) : (Off)0;
     auto gather = [&](Off v) -> Off { return g.gather32 ? (Off)((int32_t)v * (int32_t)g.a_pa) : v * (Off)g.a_pa; };
+    if (POST) {  // one source row for every term: fold it into both bases
+      const Off v = (Off)PP[(Off)(cr * g.ps0) + pi];
+      ai += gather(v);
+      bi += g.gather32 ? (Off)((int32_t)v * (int32_t)g.b_pa) : v * (Off)g.b_pa;
+    }
     Off pidx[kFusedU];
 #pragma unroll
-    for (int u = 0; u < kFusedU; ++u) pidx[u] = (perm && u < g.len) ? (Off)PP[pi + u * ps0] : (Off)0;
+    for (int u = 0; u < kFusedU; ++u) pidx[u] = (!POST && perm && u < g.len) ? (Off)PP[pi + u * ps0] : (Off)0;
     int64_t i0 = 0;
     for (; i0 + kFusedU <= g.len && (orcheck || canon); i0 += kFusedU) {
       uint64_t av[kFusedU], bv[kFusedU];
 #pragma unroll
       for (int u = 0; u < kFusedU; ++u) {
-        av[u] = (uint64_t)(int64_t)A[ai + u * a_ax + gather(pidx[u])];
+        av[u] = (uint64_t)(int64_t)A[ai + u * a_ax + (POST ? (Off)0 : gather(pidx[u]))];
         bv[u] = (uint64_t)(int64_t)B[bi + u * b_ax];
       }
       ai += kFusedU * a_ax;
       bi += kFusedU * b_ax;
-      if (perm) {
+      if (!POST && perm) {
         pi += kFusedU * ps0;
 #pragma unroll
         for (int u = 0; u < kFusedU; ++u) pidx[u] = i0 + kFusedU + u < g.len ? (Off)PP[pi + u * ps0] : (Off)0;
@@ -187,7 +199,7 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
 #pragma unroll
     for (int u = 0; u < kFusedU; ++u) {  // the last len % kFusedU terms
       if (i0 + u >= g.len) break;
-      mac((uint64_t)(int64_t)A[ai + u * a_ax + gather(pidx[u])], (uint64_t)(int64_t)B[bi + u * b_ax]);
+      mac((uint64_t)(int64_t)A[ai + u * a_ax + (POST ? (Off)0 : gather(pidx[u]))], (uint64_t)(int64_t)B[bi + u * b_ax]);
     }
     if (orcheck) canon = (ormask & himask) == 0;
     int64_t res;
@@ -195,18 +207,23 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
       res = sizeof(T) == 4 ? (int64_t)mg32_mod(lo, (const MG32 &)mc) : (int64_t)mg64_mod(hi, lo, (const MG64 &)mc);
     } else {
       res = 0;
+      const int64_t prow_v = POST ? fused_perm<PT>(g, cr, cp) : 0;
       for (int64_t i = 0; i < g.len; ++i) {
-        const int64_t aoffs = a0 + i * g.a_ax + (perm ? fused_perm<PT>(g, i, cp) * g.a_pa : 0);
-        res = exact_step<T>(res, (int64_t)A[aoffs], (int64_t)B[b0 + i * g.b_ax], q, mc);
+        const int64_t aoffs = a0 + i * g.a_ax + (POST ? prow_v * g.a_pa : perm ? fused_perm<PT>(g, i, cp) * g.a_pa : 0);
+        const int64_t boffs = b0 + i * g.b_ax + (POST ? prow_v * g.b_pa : 0);
+        res = exact_step<T>(res, (int64_t)A[aoffs], (int64_t)B[boffs], q, mc);
       }
     }
     R[r0] = (T)res;
   }
 }
 
+// post = false: modmul_axis_sum (perm_axis in the operands' axes).
+// post = true:  modmul_axis_sum_permute (perm_axis and ew in result axes).
 static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
-                 int64_t perm_axis, const heal_tensor *r, int64_t axis) {
+                 int64_t perm_axis, const heal_tensor *r, int64_t axis, bool post = false, int64_t ew = 0) {
   clear_error();
+  if (post && !perms) return set_error(HEAL_ERR_INVALID_ARGUMENT, "perms pointer must not be null.");
   HEAL_CHECK(check_desc(a, "a", true));
   HEAL_CHECK(check_desc(b, "b", true));
   HEAL_CHECK(check_desc(p, "p", true));
@@ -240,9 +257,21 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
   }
   // gathered axes: one (perms [l, m], as permute) or a pair taken as one
   // flattened axis (perms [l, m1, m2], linear across its last two axes)
-  const int gp = perms ? perms->ndim - 1 : 0;
+  const int gp = perms ? (post ? 1 : perms->ndim - 1) : 0;
   int64_t mflat = 0;
-  if (perms) {
+  int64_t paS = perm_axis;  // the gathered axis in the operands' (S) coordinates
+  if (post) {
+    // permute on the reduced result (permute_impl.cpp:19-35)
+    const int rd = nd - 1;
+    if (ew < 0 || ew >= rd || perm_axis < 0 || perm_axis >= rd)
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "Axis out of bounds.");
+    if (ew == perm_axis) return set_error(HEAL_ERR_INVALID_ARGUMENT, "elementwise_axis and perm_axis must be different.");
+    if (perms->ndim != 2 || perms->dims[0] != r->dims[ew] || perms->dims[1] != r->dims[perm_axis])
+      return set_error(HEAL_ERR_INVALID_ARGUMENT,
+                       "Perms must have shape [l, m] where l and m match a.shape at elementwise and perm axes.");
+    paS = perm_axis < axis ? perm_axis : perm_axis + 1;
+    mflat = S[paS];
+  } else if (perms) {
     if (gp < 1 || gp > 2)
       return set_error(HEAL_ERR_INVALID_ARGUMENT, "Perms must have shape [l, m] (or [l, m1, m2] for two axes).");
     if (perm_axis < 0 || perm_axis + gp > nd) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Axis out of bounds.");
@@ -263,13 +292,15 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
   const int64_t n = numel(*r);
   if (n == 0) return HEAL_OK;
   heal_tensor PV;  // perms as [l, m1 * m2]
-  if (perms) {
+  if (post) {
+    PV = *perms;
+  } else if (perms) {
     PV = *perms;
     PV.ndim = 2;
     PV.dims[1] = mflat;
     PV.strides[1] = (gp == 2 && perms->dims[2] == 1) ? perms->strides[1] : perms->strides[gp];
   }
-  if (perms && S[axis] > 0) {
+  if (perms && (post || S[axis] > 0)) {
     bool valid = false;
     HEAL_CHECK(perms_valid(PV, mflat, &valid));
     if (!valid) return set_error(HEAL_ERR_OUT_OF_RANGE, "Permutation index out of bounds.");
@@ -295,7 +326,7 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
       as[i] = (ia >= 0 && A.dims[ia] != 1) ? A.strides[ia] : 0;
       bs[i] = (ib >= 0 && B.dims[ib] != 1) ? B.strides[ib] : 0;
     }
-    if (gp == 2 && S[perm_axis + 1] > 1 && as[perm_axis] != as[perm_axis + 1] * S[perm_axis + 1]) {
+    if (!post && gp == 2 && S[perm_axis + 1] > 1 && as[perm_axis] != as[perm_axis + 1] * S[perm_axis + 1]) {
       rc = set_error(HEAL_ERR_INVALID_ARGUMENT, "a must be linear across the two gathered axes.");
     } else {
       g.r = make_view(*r);
@@ -303,34 +334,37 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
       g.bo = g.r;
       for (int i = 0, j = 0; i < nd; ++i) {
         if (i == axis) continue;
-        const bool gathered = perms && i >= perm_axis && i < perm_axis + gp;
+        const bool gathered = perms && i >= paS && i < paS + gp;
         g.ao.strides[j] = gathered ? 0 : as[i];
-        g.bo.strides[j] = bs[i];
+        g.bo.strides[j] = (post && gathered) ? 0 : bs[i];
         ++j;
       }
       g.a_ax = as[axis];
       g.b_ax = bs[axis];
       g.len = S[axis];
       // stride of the flattened gathered index: the inner axis's (the outer's if the inner has length 1)
-      g.a_pa = !perms ? 0 : (gp == 2 && S[perm_axis + 1] == 1) ? as[perm_axis] : as[perm_axis + gp - 1];
-      const int pa = perms ? (int)(perm_axis < axis ? perm_axis : perm_axis - 1) : -1;
+      g.a_pa = !perms ? 0 : post ? as[paS] : (gp == 2 && S[perm_axis + 1] == 1) ? as[perm_axis] : as[perm_axis + gp - 1];
+      g.b_pa = post ? bs[paS] : 0;
+      const int pa = post ? (int)perm_axis : perms ? (int)(perm_axis < axis ? perm_axis : perm_axis - 1) : -1;
       const int last = nd - 2;
       // merge axes other than the ones whose coordinates the kernel reads
       unsigned keep = 1u << last;
       if (pa >= 0) keep |= 1u << pa;
       if (gp == 2) keep |= 1u << (pa + 1);
+      if (post) keep |= 1u << ew;
       View *vs[3] = {&g.r, &g.ao, &g.bo};
       int map[HEAL_MAX_DIMS];
       coalesce_views(vs, 3, keep, map);
       g.pa = pa >= 0 ? map[pa] : -1;
       g.pa2 = gp == 2 ? map[pa + 1] : -1;
+      g.prow = post ? map[ew] : -1;
       g.last = map[last];
       make_fast_dims(g.r, n, &g.fd);
       g.ps0 = perms ? PR.strides[0] : 0;
       g.ps1 = perms ? PR.strides[1] : 0;
       // indices are validated to lie in [0, mflat)
-      g.gather32 = perms && g.a_pa >= 0 && mflat > 0 &&
-                   (__int128)g.a_pa * (__int128)(mflat - 1) < ((__int128)1 << 31);
+      g.gather32 = perms && g.a_pa >= 0 && g.b_pa >= 0 && mflat > 0 &&
+                   (__int128)std::max(g.a_pa, g.b_pa) * (__int128)(mflat - 1) < ((__int128)1 << 31);
       g.a = A.data;
       g.b = B.data;
       g.perms = perms ? PR.data : nullptr;
@@ -348,7 +382,7 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
     return s < ((__int128)1 << 31) - 1;
   };
   const bool off32 = span_ok(A) && span_ok(B) && (!perms || span_ok(PR)) && g.a_ax >= 0 && g.b_ax >= 0 &&
-                     g.ps0 >= 0 && g.ps1 >= 0 && g.a_pa >= 0;
+                     g.ps0 >= 0 && g.ps1 >= 0 && g.a_pa >= 0 && g.b_pa >= 0;
   if (!rc) {
     const int threads = 256;
     const int64_t want = (n + threads - 1) / threads;
@@ -357,8 +391,13 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
     auto go = [&](auto t_tag, auto p_tag) {
       typedef decltype(t_tag) TT;
       typedef decltype(p_tag) PTT;
-      if (off32) modmul_axis_sum_kernel<TT, PTT, int32_t><<<grid, threads, 0, stream()>>>(g);
-      else modmul_axis_sum_kernel<TT, PTT, int64_t><<<grid, threads, 0, stream()>>>(g);
+      if (post) {
+        if (off32) modmul_axis_sum_kernel<TT, PTT, int32_t, true><<<grid, threads, 0, stream()>>>(g);
+        else modmul_axis_sum_kernel<TT, PTT, int64_t, true><<<grid, threads, 0, stream()>>>(g);
+      } else {
+        if (off32) modmul_axis_sum_kernel<TT, PTT, int32_t, false><<<grid, threads, 0, stream()>>>(g);
+        else modmul_axis_sum_kernel<TT, PTT, int64_t, false><<<grid, threads, 0, stream()>>>(g);
+      }
     };
     if (dt == HEAL_INT32) {
       if (p32) go(int32_t(), int32_t());
@@ -367,7 +406,7 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
       if (p32) go(int64_t(), int32_t());
       else go(int64_t(), int64_t());
     }
-    rc = check_launch("modmul_axis_sum");
+    rc = check_launch(post ? "modmul_axis_sum_permute" : "modmul_axis_sum");
   }
   for (void *o : owned) scratch_free(o);
   if (!rc) mark_written(r->data);
@@ -383,6 +422,12 @@ extern "C" {
 int heal_modmul_axis_sum(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
                          int64_t perm_axis, const heal_tensor *result, int64_t axis) {
   return fused(a, b, p, perms, perm_axis, result, axis);
+}
+
+int heal_modmul_axis_sum_permute(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, int64_t axis,
+                                 const heal_tensor *perms, int64_t elementwise_axis, int64_t perm_axis,
+                                 const heal_tensor *result) {
+  return fused(a, b, p, perms, perm_axis, result, axis, true, elementwise_axis);
 }
 
 }  // extern "C"

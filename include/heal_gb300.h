@@ -267,6 +267,24 @@ int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tens
 int heal_modmul_axis_sum(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
                          int64_t perm_axis, const heal_tensor *result, int64_t axis);
 
+/* The tail of a keyswitch in one pass (an extension: HEAL has no such op).
+ * Defined as the composition of HEAL's own calls
+ *   result = permute(axis_modsum(modmul(a, b, p), axis), perms,
+ *                    elementwise_axis, perm_axis)
+ * (example_impl/modop_impl.cpp:44-101, axis_modsum_impl.cpp:12-76,
+ * permute_impl.cpp:8-65): a and b broadcast like modmul to a common shape S,
+ * axis in [0, ndim(S) - 2], p of shape [S[-1]], and elementwise_axis /
+ * perm_axis numbered in result's axes (S without `axis`), perms of shape
+ * [result.dims[elementwise_axis], result.dims[perm_axis]].  A permutation
+ * gathers whole rows along perm_axis, so each result element is the running
+ * sum over `axis` of a * b at its source row; the product and the unpermuted
+ * sum are never written.  Bit-identical to the three calls.  Errors as
+ * modmul / axis_modsum / permute; indices are checked before anything is
+ * written. */
+int heal_modmul_axis_sum_permute(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, int64_t axis,
+                                 const heal_tensor *perms, int64_t elementwise_axis, int64_t perm_axis,
+                                 const heal_tensor *result);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

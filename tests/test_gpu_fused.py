@@ -150,3 +150,88 @@ def test_argument_errors():
     for args, exc in bad:
         with pytest.raises(exc):
             capi.call("heal_modmul_axis_sum", *args)
+
+
+# ------------------------------------------- heal_modmul_axis_sum_permute
+def fused_post(a, b, p, axis, perms, ew, pa, out=None):
+    shape = np.broadcast_shapes(a.shape, b.shape)
+    out_shape = tuple(d for i, d in enumerate(shape) if i != axis)
+    o = out if out is not None else capi.DeviceArray.empty(out_shape, a.dtype)
+    capi.call("heal_modmul_axis_sum_permute", a if isinstance(a, capi.DeviceArray) else up(a),
+              b if isinstance(b, capi.DeviceArray) else up(b), up(p), axis, up(perms), ew, pa, o)
+    return o.numpy()
+
+
+def composed_post(a, b, p, axis, perms, ew, pa):
+    shape = np.broadcast_shapes(a.shape, b.shape)
+    prod = O.modmul(np.ascontiguousarray(np.broadcast_to(a, shape)),
+                    np.ascontiguousarray(np.broadcast_to(b, shape)), p, out_shape=shape)
+    return O.permute(O.axis_modsum(prod, p, axis), perms.astype(a.dtype), ew, pa)
+
+
+def random_perms(rng, rows, m, dt):
+    return np.stack([rng.permutation(m) for _ in range(rows)]).astype(dt)
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+@pytest.mark.parametrize("shapes,axis,ew,pa", [
+    (((2, 64, 1, 3, 5), (2, 64, 1, 3, 5)), 3, 2, 1),     # keyswitch tail: digits reduced, rows gathered
+    (((2, 64, 1, 3, 5), (1, 64, 1, 3, 5)), 3, 0, 1),     # b broadcast over the components
+    (((7, 33, 4), (7, 33, 4)), 0, 1, 0),                 # gathered axis after the reduced one
+    (((5, 9, 6, 4), (9, 1, 4)), 2, 0, 1),                # broadcast b, reduced axis after the gathered one
+    (((3, 50, 2), (3, 50, 2)), 0, 1, 0),
+])
+def test_post_permute_matches_composition(dt, shapes, axis, ew, pa):
+    rng = np.random.default_rng(31)
+    sa, sb = shapes
+    p = moduli(dt, sa[-1], rng)
+    a = (rng.integers(0, 1 << 62, size=sa) % p.astype(np.int64)).astype(dt)
+    b = (rng.integers(0, 1 << 62, size=sb) % p.astype(np.int64)).astype(dt)
+    shape = np.broadcast_shapes(sa, sb)
+    rshape = tuple(d for i, d in enumerate(shape) if i != axis)
+    perms = random_perms(rng, rshape[ew], rshape[pa], np.int64)
+    assert np.array_equal(fused_post(a, b, p, axis, perms, ew, pa), composed_post(a, b, p, axis, perms, ew, pa))
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+def test_post_permute_non_canonical_and_duplicate_rows(dt):
+    rng = np.random.default_rng(32)
+    p = np.array([97, 65521, 7], dtype=dt)
+    a = rng.integers(-1000, 100000, size=(2, 40, 1, 3, 3)).astype(dt)
+    b = rng.integers(-500, 3000, size=(2, 40, 1, 3, 3)).astype(dt)
+    perms = random_perms(rng, 1, 40, np.int32)
+    perms[0, 7] = perms[0, 8]                          # two results read one row
+    assert np.array_equal(fused_post(a, b, p, 3, perms, 2, 1), composed_post(a, b, p, 3, perms, 2, 1))
+
+
+def test_post_permute_is_the_keyswitch_tail():
+    from heal_gb300.chain import KeyswitchChain
+    ch = KeyswitchChain(n=1024, limbs=4, digits=3, base_bits=17, bound_bits=50)
+    ct = capi.DeviceArray.from_numpy(P.residues(41, ch.shape(), ch.qs))
+    want = capi.DeviceArray.empty(ch.shape(), np.int64)
+    got = capi.DeviceArray.empty(ch.shape(), np.int64)
+    ch.run(ct, want)
+    for _ in range(2):
+        ch.run_fused(ct, got)
+        assert np.array_equal(got.numpy(), want.numpy())
+
+
+def test_post_permute_errors():
+    p = np.array([97, 89], np.int64)
+    a = np.zeros((3, 4, 2), np.int64)
+    out = capi.DeviceArray.empty((4, 2), np.int64)           # result of a [3, 4, 2] reduced over axis 0
+    L = capi.lib()
+    ok = up(np.tile(np.arange(4), (2, 1)).astype(np.int64))  # [result.dims[ew = 1], result.dims[pa = 0]]
+    perms = np.tile(np.arange(4), (3, 1)).astype(np.int64)   # wrong shape: [3, 4]
+    da, dp = up(a), up(p)
+    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(ok), 1, 0, capi._arg(out)) == 0
+    bad_axes = [(0, 0), (2, 0), (1, 5)]
+    for ew, pa in bad_axes:
+        assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(ok), ew, pa, capi._arg(out)) == 1
+    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(up(perms)), 1, 0, capi._arg(out)) == 1
+    oob = np.tile(np.arange(4), (2, 1)).astype(np.int64)
+    oob[1, 3] = 4
+    before = out.numpy().copy()
+    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(up(oob)), 1, 0, capi._arg(out)) == 2
+    assert np.array_equal(out.numpy(), before)              # nothing written
+    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, None, 1, 0, capi._arg(out)) == 1
