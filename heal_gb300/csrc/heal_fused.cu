@@ -218,6 +218,94 @@ __global__ void __launch_bounds__(256) modmul_axis_sum_kernel(const __grid_const
   }
 }
 
+// ------------------------------------------------ lean post-permute form
+// The same composition for the common case of a short reduced axis (the
+// digits of a keyswitch): every offset fits 31 bits, the result view has at
+// most 4 axes after merging, and the reduced axis has D <= 4 terms.  One
+// thread per result element; axis roles enter as 0/1 multipliers instead of
+// per-axis selects, and all 2D term loads are issued before the products.
+struct TailArgs {
+  const void *a, *b, *perms, *ptab;
+  void *out;
+  uint32_t n;                  // result elements
+  int nd;                      // result view axes (1..4)
+  FastDiv fd[4];               // result view dims
+  int32_t as[4], bs[4], rs[4]; // strides in result coordinates (0 for a and b on the gathered axis)
+  int32_t ew_m[4], pa_m[4], t_m[4];  // 1 on the elementwise / gathered / last axis
+  int32_t a_ax, b_ax, a_pa, b_pa, ps0, ps1;
+  Diag *diag;
+};
+
+template <typename T, typename PT, int D>
+__global__ void __launch_bounds__(256) tail_kernel(const __grid_constant__ TailArgs g) {
+  typedef typename FusedMG<T>::type M;
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n) return;
+  uint32_t rem = idx;
+  int32_t ao = 0, bo = 0, ro = 0, cr = 0, cp = 0, t = 0;
+#pragma unroll
+  for (int k = 3; k >= 0; --k) {
+    if (k >= g.nd) continue;
+    const uint32_t qd = fastdiv(rem, g.fd[k]);
+    const int32_t c = (int32_t)(rem - qd * g.fd[k].d);
+    rem = qd;
+    ao += c * g.as[k];
+    bo += c * g.bs[k];
+    ro += c * g.rs[k];
+    cr += c * g.ew_m[k];
+    cp += c * g.pa_m[k];
+    t += c * g.t_m[k];
+  }
+  const int32_t v = (int32_t)((const PT *)g.perms)[cr * g.ps0 + cp * g.ps1];  // validated: 0 <= v < m
+  const T *A = (const T *)g.a + (ao + v * g.a_pa);
+  const T *B = (const T *)g.b + (bo + v * g.b_pa);
+  int64_t av[D], bv[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    av[i] = (int64_t)A[i * g.a_ax];
+    bv[i] = (int64_t)B[i * g.b_ax];
+  }
+  const M mc = ((const M *)g.ptab)[t];
+  const int64_t q = sizeof(T) == 4 ? (int64_t)(int32_t)((const MG32 &)mc).q : (int64_t)((const MG64 &)mc).q;
+  T *R = (T *)g.out;
+  if (q == 0) {
+    atomicAdd(&g.diag->zero_mod, 1ull);
+    R[ro] = 0;
+    return;
+  }
+  // canonical terms: (sum of products) mod q, accumulated exactly
+  bool canon = q > 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) canon = canon && av[i] >= 0 && av[i] < q && bv[i] >= 0 && bv[i] < q;
+  int64_t res;
+  if (canon) {
+    if (sizeof(T) == 4) {
+      uint64_t lo = 0;  // D < 4 products below q^2 < 2^62: no overflow
+#pragma unroll
+      for (int i = 0; i < D; ++i) lo += (uint64_t)av[i] * (uint64_t)bv[i];
+      res = (int64_t)mg32_mod(lo, (const MG32 &)mc);
+    } else {
+      const uint64_t uq = (uint64_t)q;
+      uint64_t hi = 0, lo = 0;  // hi * 2^64 + lo, hi < q
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        const uint64_t x = (uint64_t)av[i], y = (uint64_t)bv[i];
+        const uint64_t plo = x * y, phi = mulhi64(x, y);
+        const uint64_t s = lo + plo;
+        hi += phi + (s < lo ? 1 : 0);
+        lo = s;
+        hi = hi >= uq ? hi - uq : hi;
+      }
+      res = (int64_t)mg64_mod(hi, lo, (const MG64 &)mc);
+    }
+  } else {
+    res = 0;
+#pragma unroll
+    for (int i = 0; i < D; ++i) res = exact_step<T>(res, av[i], bv[i], q, mc);
+  }
+  R[ro] = (T)res;
+}
+
 // post = false: modmul_axis_sum (perm_axis in the operands' axes).
 // post = true:  modmul_axis_sum_permute (perm_axis and ew in result axes).
 static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
@@ -383,7 +471,59 @@ static int fused(const heal_tensor *a, const heal_tensor *b, const heal_tensor *
   };
   const bool off32 = span_ok(A) && span_ok(B) && (!perms || span_ok(PR)) && g.a_ax >= 0 && g.b_ax >= 0 &&
                      g.ps0 >= 0 && g.ps1 >= 0 && g.a_pa >= 0 && g.b_pa >= 0;
-  if (!rc) {
+  // the lean post-permute kernel where its limits hold
+  bool lean = !rc && post && off32 && g.fd.fast && g.r.ndim <= 4 && g.len >= 1 && g.len <= 4 &&
+              n < ((int64_t)1 << 32) && g.a_pa >= 0 && g.b_pa >= 0;
+  TailArgs ta;
+  memset(&ta, 0, sizeof ta);
+  if (lean) {
+    ta.nd = g.r.ndim;
+    for (int k = 0; k < g.r.ndim; ++k) {
+      lean = lean && g.r.strides[k] >= 0 && g.ao.strides[k] >= 0 && g.bo.strides[k] >= 0;
+      ta.fd[k] = g.fd.fd[k];
+      ta.as[k] = (int32_t)g.ao.strides[k];
+      ta.bs[k] = (int32_t)g.bo.strides[k];
+      ta.rs[k] = (int32_t)g.r.strides[k];
+      ta.ew_m[k] = k == g.prow;
+      ta.pa_m[k] = k == g.pa;
+      ta.t_m[k] = k == g.last;
+    }
+    ta.a = g.a;
+    ta.b = g.b;
+    ta.perms = g.perms;
+    ta.ptab = g.ptab;
+    ta.out = g.out;
+    ta.n = (uint32_t)n;
+    ta.a_ax = (int32_t)g.a_ax;
+    ta.b_ax = (int32_t)g.b_ax;
+    ta.a_pa = (int32_t)g.a_pa;
+    ta.b_pa = (int32_t)g.b_pa;
+    ta.ps0 = (int32_t)g.ps0;
+    ta.ps1 = (int32_t)g.ps1;
+    ta.diag = g.diag;
+  }
+  if (lean) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    const bool p32 = g.perms_dtype == HEAL_INT32;
+    auto go = [&](auto t_tag, auto p_tag) {
+      typedef decltype(t_tag) TT;
+      typedef decltype(p_tag) PTT;
+      switch (g.len) {
+        case 1: tail_kernel<TT, PTT, 1><<<blocks, 256, 0, stream()>>>(ta); break;
+        case 2: tail_kernel<TT, PTT, 2><<<blocks, 256, 0, stream()>>>(ta); break;
+        case 3: tail_kernel<TT, PTT, 3><<<blocks, 256, 0, stream()>>>(ta); break;
+        default: tail_kernel<TT, PTT, 4><<<blocks, 256, 0, stream()>>>(ta); break;
+      }
+    };
+    if (dt == HEAL_INT32) {
+      if (p32) go(int32_t(), int32_t());
+      else go(int32_t(), int64_t());
+    } else {
+      if (p32) go(int64_t(), int32_t());
+      else go(int64_t(), int64_t());
+    }
+    rc = check_launch("modmul_axis_sum_permute");
+  } else if (!rc) {
     const int threads = 256;
     const int64_t want = (n + threads - 1) / threads;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)device_sm_count() * 16));
