@@ -404,6 +404,16 @@ void modmul_axis_sum(const std::shared_ptr<DeviceTensor<T>> &a, const std::share
   check(heal_modmul_axis_sum(&A, &B, &P, perms ? &PM : nullptr, perm_axis, &R, axis));
 }
 
+template <typename T>
+void modmul_axis_sum_permute(const std::shared_ptr<DeviceTensor<T>> &a, const std::shared_ptr<DeviceTensor<T>> &b,
+                             const std::shared_ptr<DeviceTensor<T>> &p, int64_t axis,
+                             const std::shared_ptr<DeviceTensor<T>> &perms, int64_t elementwise_axis,
+                             int64_t perm_axis, std::shared_ptr<DeviceTensor<T>> &result) {
+  heal_tensor A = need(a, "a"), B = need(b, "b"), P = need(p, "p"), PM = need(perms, "perms"),
+              R = need(result, "result");
+  check(heal_modmul_axis_sum_permute(&A, &B, &P, axis, &PM, elementwise_axis, perm_axis, &R));
+}
+
 void synchronize() { check(heal_synchronize()); }
 
 // ============================================================ instantiations
@@ -444,6 +454,11 @@ void synchronize() { check(heal_synchronize()); }
   template void modmul_axis_sum<T>(const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
                                    const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
                                    int64_t, std::shared_ptr<DeviceTensor<T>> &, int64_t);                           \
+  template void modmul_axis_sum_permute<T>(const std::shared_ptr<DeviceTensor<T>> &,                              \
+                                           const std::shared_ptr<DeviceTensor<T>> &,                              \
+                                           const std::shared_ptr<DeviceTensor<T>> &, int64_t,                     \
+                                           const std::shared_ptr<DeviceTensor<T>> &, int64_t, int64_t,            \
+                                           std::shared_ptr<DeviceTensor<T>> &);                                   \
   template void axis_modsum<T>(const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
                                std::shared_ptr<DeviceTensor<T>> &, int64_t);                                    \
   template void g_decomposition<T>(const std::shared_ptr<DeviceTensor<T>> &, std::shared_ptr<DeviceTensor<T>> &,  \

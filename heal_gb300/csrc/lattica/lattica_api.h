@@ -127,6 +127,13 @@ template <typename T>
 void modmul_axis_sum(const std::shared_ptr<DeviceTensor<T>> &a, const std::shared_ptr<DeviceTensor<T>> &b,
                      const std::shared_ptr<DeviceTensor<T>> &p, const std::shared_ptr<DeviceTensor<T>> &perms,
                      int64_t perm_axis, std::shared_ptr<DeviceTensor<T>> &result, int64_t axis);
+// result = permute(axis_modsum(modmul(a, b, p), axis), perms, elementwise_axis,
+// perm_axis) in one pass (an extension; see heal_modmul_axis_sum_permute).
+template <typename T>
+void modmul_axis_sum_permute(const std::shared_ptr<DeviceTensor<T>> &a, const std::shared_ptr<DeviceTensor<T>> &b,
+                             const std::shared_ptr<DeviceTensor<T>> &p, int64_t axis,
+                             const std::shared_ptr<DeviceTensor<T>> &perms, int64_t elementwise_axis,
+                             int64_t perm_axis, std::shared_ptr<DeviceTensor<T>> &result);
 template <typename T>
 std::shared_ptr<DeviceTensor<T>> get_slice(const std::shared_ptr<DeviceTensor<T>> &tensor, int64_t axis,
                                            int64_t start, int64_t stop, int64_t step);

@@ -17,6 +17,7 @@ the others are:
   apply_g_decomp(a, power, base_bits, out)            HEAL g_decomposition
   take_along_axis(a, perms, elementwise_axis, perm_axis, out)   HEAL permute
   modmul_axis_sum(a, b, p, axis, out, perms=None, perm_axis=0)
+  modmul_axis_sum_permute(a, b, p, axis, perms, elementwise_axis, perm_axis, out)   (extension)
   moveaxis(a, source, destination)                    a new view
   get_slice(a, *index)                                ints, slices (step > 0), Ellipsis; a new view
   new_reference(a)                                    a new view of the same tensor
@@ -111,6 +112,12 @@ class GB300Dispatcher:
 
     def modmul_axis_sum(self, a, b, p, axis, out, perms=None, perm_axis=0):
         self._f("modmul_axis_sum", a)(a, b, p, perms, perm_axis, out, axis)
+        return out
+
+    def modmul_axis_sum_permute(self, a, b, p, axis, perms, elementwise_axis, perm_axis, out):
+        """permute(axis_modsum(modmul(a, b, p), axis), perms, elementwise_axis,
+        perm_axis) in one call (an extension op of this backend)."""
+        self._f("modmul_axis_sum_permute", a)(a, b, p, axis, perms, elementwise_axis, perm_axis, out)
         return out
 
     def apply_g_decomp(self, a, power, base_bits, out):

@@ -235,3 +235,24 @@ def test_post_permute_errors():
     assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(up(oob)), 1, 0, capi._arg(out)) == 2
     assert np.array_equal(out.numpy(), before)              # nothing written
     assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, None, 1, 0, capi._arg(out)) == 1
+
+
+def test_post_permute_through_lattica_hw():
+    """The same op through the `lattica_hw` module and the transcript dispatcher."""
+    import torch
+    import heal_gb300
+    from heal_gb300.runtime.dispatcher import GB300Dispatcher
+    hw = heal_gb300.lattica_hw()
+    rng = np.random.default_rng(33)
+    p = np.array([65537, 97, 257], np.int64)
+    a = (rng.integers(0, 1 << 40, size=(2, 16, 1, 3, 3)) % p).astype(np.int64)
+    b = (rng.integers(0, 1 << 40, size=(2, 16, 1, 3, 3)) % p).astype(np.int64)
+    perms = random_perms(rng, 1, 16, np.int64)
+    want = composed_post(a, b, p, 3, perms, 2, 1)
+    H = lambda x: hw.host_to_device_64(torch.from_numpy(np.ascontiguousarray(x)))
+    out = hw.allocate_on_hardware_64([2, 16, 1, 3])
+    hw.modmul_axis_sum_permute_64(H(a), H(b), H(p), 3, H(perms), 2, 1, out)
+    assert np.array_equal(hw.device_to_host_64(out).numpy(), want)
+    out2 = hw.allocate_on_hardware_64([2, 16, 1, 3])
+    GB300Dispatcher().modmul_axis_sum_permute(H(a), H(b), H(p), 3, H(perms), 2, 1, out2)
+    assert np.array_equal(hw.device_to_host_64(out2).numpy(), want)
