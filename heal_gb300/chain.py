@@ -10,7 +10,7 @@ the 2 ciphertext components as l and the L RNS limbs as k):
   acc   = axis_modsum(prod viewed [2, N, 1, D, L], p, axis=3)
   out   = permute(acc, galois[1, N], elementwise_axis=2, perm_axis=1)
 
-(run_fused replaces the last three calls with one heal_modmul_axis_sum_permute.)
+(run_fused makes 3 calls: intt, heal_g_decomposition_ntt, heal_modmul_axis_sum_permute.)
 Every step is one C-ABI call (include/heal_gb300.h); the reshape and the
 digit-axis move are stride-only views.  The moduli are the L largest primes
 q < 2^bound_bits with q = 1 (mod 2N); the key is seeded uniform residues; the
@@ -90,23 +90,24 @@ class KeyswitchChain:
         capi.call("heal_permute", self.acc, d["gal"], out, 2, 1)
 
     def run_fused(self, ct: capi.DeviceArray, out: capi.DeviceArray):
-        """The same step with its tail fused: modmul, axis_modsum and permute
-        as one heal_modmul_axis_sum_permute call on the NTT digits and the key
-        (bit-identical to run(); the product and the digit sum are never
-        written).  4 HEAL calls."""
+        """The same step in 3 HEAL-level calls: the INTT, then
+        heal_g_decomposition_ntt (the digit NTT extracts the digits as it
+        loads x, so the digit tensor is never written), then
+        heal_modmul_axis_sum_permute (modmul, axis_modsum and permute in one
+        pass).  Bit-identical to run()."""
         d = self.dev
         capi.call("heal_intt", ct, d["p"], d["perm"], d["itw"], d["minv"], None, None, self.x)
-        capi.call("heal_g_decomposition", self.x, self.dig, self.D, self.bits)
-        capi.call("heal_ntt", self.dig_flat, d["p_t"], d["perm"], d["tw_t"], None, None, self.dn)
+        capi.call("heal_g_decomposition_ntt", self.x, self.D, self.bits, d["p_t"], d["perm"], d["tw_t"], self.dn)
         capi.call("heal_modmul_axis_sum_permute", self.prod_moved, self.key_moved, d["p"], 3, d["gal"], 2, 1, out)
 
     def bytes_per_chain_fused(self) -> int:
-        """Algorithmic bytes of run_fused: the first three calls as in run(),
-        then one read of the digits and the key and one write of the result."""
+        """Algorithmic bytes of run_fused: the INTT's read and write, the
+        digit NTT's read of x and write of the digit transforms, and one read
+        of those and the key and one write of the result."""
         e = self.dtype.itemsize
         ct = 2 * self.n * self.L * e
         dg = ct * self.D
-        return (2 * ct) + (ct + dg) + (2 * dg) + (2 * dg + ct)
+        return (2 * ct) + (ct + dg) + (2 * dg + ct)
 
     # ---- algorithmic bytes (reads + writes of the six calls, tables excluded)
     def bytes_per_chain(self) -> int:

@@ -213,6 +213,31 @@ HEAL_HD uint32_t fastdiv(uint32_t n, const FastDiv &f) {
   return (t1 + ((n - t1) >> f.s1)) >> f.s2;
 }
 
+// -------------------------------------------------------- g_decomposition
+// Digit d of `value` after d of the reference's steps (remainder and
+// quotient of the value by the size_t base, quotient stored back in T;
+// example_impl/g_decomposition_impl.cpp:17,52-58), in closed form.  int64: the
+// first quotient is already non-negative, so the steps are logical shifts of
+// the uint64 image.  int32: storing uv >> bits back into an int32 is an
+// arithmetic shift of the int32 value (saturating at 31).
+template <typename T>
+HEAL_HD uint64_t gdec_digit(int64_t value, uint64_t d, uint64_t bits, uint64_t mask) {
+  const uint64_t sh = d * bits;
+  if (sizeof(T) == 4) {
+    const int32_t v = (int32_t)value >> (sh > 31 ? 31 : sh);
+    return (uint64_t)(int64_t)v & mask;
+  }
+  const uint64_t uv = (uint64_t)value;
+  return (sh >= 64 ? 0 : (uv >> sh)) & mask;
+}
+
+// The residual after `power` steps as the reference's `value > 0` test sees it.
+template <typename T>
+HEAL_HD int64_t gdec_residual(int64_t value, uint64_t power, uint64_t bits) {
+  const int64_t rest = (int64_t)gdec_digit<T>(value, power, bits, ~0ull);
+  return sizeof(T) == 4 ? (int64_t)(int32_t)(uint32_t)rest : rest;
+}
+
 // -------------------------------------------------------------- exact C
 // C's truncating remainder in the double-width type.
 HEAL_HD int64_t crem128(i128 a, int64_t q) { return (int64_t)(a % (i128)q); }

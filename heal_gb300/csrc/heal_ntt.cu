@@ -49,6 +49,8 @@ int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, int mode);
 int launch_ntt_pass_fwd64(const NttArgs &a, int64_t nblocks, int mode);
 int launch_ntt_pass_inv32(const NttArgs &a, int64_t nblocks, int mode);
 int launch_ntt_pass_inv64(const NttArgs &a, int64_t nblocks, int mode);
+int launch_ntt_pass_fwd32_gdec(const NttArgs &a, int64_t nblocks, int mode);
+int launch_ntt_pass_fwd64_gdec(const NttArgs &a, int64_t nblocks, int mode);
 
 // out[i, u, j, t] = src[i, perm[u], j, t] (forward NTT with a non-bijective
 // permutation after the two-pass transform)
@@ -70,6 +72,7 @@ __global__ void __launch_bounds__(256) ntt_gather_kernel(const T *src, int64_t s
 // ----------------------------------------------------------- host side
 static int launch_any(const NttArgs &a, int64_t nblocks, bool is32, int mode, bool inv) {
   if (inv) return is32 ? launch_ntt_pass_inv32(a, nblocks, mode) : launch_ntt_pass_inv64(a, nblocks, mode);
+  if (a.gdec_power) return is32 ? launch_ntt_pass_fwd32_gdec(a, nblocks, mode) : launch_ntt_pass_fwd64_gdec(a, nblocks, mode);
   return is32 ? launch_ntt_pass_fwd32(a, nblocks, mode) : launch_ntt_pass_fwd64(a, nblocks, mode);
 }
 
@@ -124,10 +127,33 @@ static bool plan_valid(const NttPlan &pl, int logm) {
   return pl.first_log >= 1 && pl.first_log <= kSinglePassLogMax && second >= 1 && second <= kSinglePassLogMax;
 }
 
-static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm,
-                   const heal_tensor *tw, const heal_tensor *minv, const heal_tensor *res) {
+// g_decomposition fused into the forward transform's first load
+// (heal_g_decomposition_ntt): the transform runs on the digit tensor
+// [l, m, r, k * power] that g_decomposition(a, power, bits) reshaped would be.
+struct GdecSpec {
+  int64_t power, bits;
+};
+
+static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, const heal_tensor *perm,
+                   const heal_tensor *tw, const heal_tensor *minv, const heal_tensor *res,
+                   const GdecSpec *gd = nullptr) {
   clear_error();
-  HEAL_CHECK(check_desc(a, "a", true));
+  HEAL_CHECK(check_desc(a_in, "a", true));
+  heal_tensor Av;  // the transform's input shape (the digit tensor's, with g_decomposition)
+  const heal_tensor *a = a_in;
+  if (gd) {
+    HEAL_CHECK(check_desc(res, "result", true));
+    if (gd->bits < 0 || gd->bits >= 64) return set_error(HEAL_ERR_INVALID_ARGUMENT, "base_bits must be below 64");
+    if (gd->power < 1 || gd->power > (1 << 20))
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "power must be in 1 .. 2^20");
+    if (a_in->ndim != 4) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Input tensor 'a' must have shape [l, m, r, k].");
+    bool ok = res->ndim == 4 && res->dims[3] == a_in->dims[3] * gd->power;
+    for (int i = 0; ok && i < 3; ++i) ok = res->dims[i] == a_in->dims[i];
+    if (!ok) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Output must have shape [l, m, r, k * power].");
+    Av = *a_in;
+    Av.dims[3] = a_in->dims[3] * gd->power;
+    a = &Av;
+  }
   HEAL_CHECK(check_desc(p, "p", true));
   HEAL_CHECK(check_desc(perm, "perm", true));
   HEAL_CHECK(check_desc(tw, inv ? "inv_twiddles" : "twiddles", true));
@@ -185,9 +211,9 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   HEAL_CHECK(twiddle_table(*tw, *p, wide, &tt));
   if (inv) HEAL_CHECK(minv_table(*minv, *p, k, wide, &mt));
 
-  heal_tensor A = *a;
+  heal_tensor A = *a_in;  // the source as stored (with g_decomposition: the undecomposed tensor)
   void *owned_a = nullptr;
-  if (overlaps(A, *res) && !identical_view(A, *res)) HEAL_CHECK(materialize(A, &A, &owned_a));
+  if (overlaps(A, *res) && (gd || !identical_view(A, *res))) HEAL_CHECK(materialize(A, &A, &owned_a));
 
   NttArgs base;
   memset(&base, 0, sizeof base);
@@ -204,6 +230,7 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
   base.q = mi.q;
   base.qone = mi.qone;
   base.bitrev = pi.bitrev_log;  // every table this call indexes is the bit reversal (its own inverse)
+  base.diag = diag_device();
   if (inv) {
     base.minv_pairs = mt.pairs;
     base.minv_neg = mt.neg_flag;
@@ -255,6 +282,10 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
     } else {
       x.store_gather = pi.perm32;
     }
+    if (gd) {
+      x.gdec_power = (int)gd->power;
+      x.gdec_bits = (int)gd->bits;
+    }
     rc = launch_any(x, nb, is32, mode_of(logm), inv);
   } else {
     // two passes through a dense [l, m, r, k] scratch tensor
@@ -279,6 +310,10 @@ static int ntt_run(bool inv, const heal_tensor *a, const heal_tensor *p, const h
       // second runs the register kernel (at least 3 stages)
       const int m1 = mode_of(p1), m2 = mode_of(p2);
       x.lazy_out = m1 == MODE_W64_GROW && m2 == MODE_W64_GROW && p2 >= 3;
+      if (gd) {
+        x.gdec_power = (int)gd->power;
+        x.gdec_bits = (int)gd->bits;
+      }
       rc = launch_any(x, nb, is32, m1, false);
       if (!rc) {
         NttArgs y = base;  // pass 2: remaining stages on contiguous blocks
@@ -357,6 +392,12 @@ int heal_ntt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm
   (void)log2p;
   (void)mu;  // optional Barrett inputs (include/ntt.h:24-26); Shoup needs neither
   return ntt_run(false, a, p, perm, twiddles, nullptr, result);
+}
+
+int heal_g_decomposition_ntt(const heal_tensor *a, int64_t power, int64_t base_bits, const heal_tensor *p,
+                             const heal_tensor *perm, const heal_tensor *twiddles, const heal_tensor *result) {
+  const GdecSpec gd{power, base_bits};
+  return ntt_run(false, a, p, perm, twiddles, nullptr, result, &gd);
 }
 
 int heal_intt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm, const heal_tensor *inv_twiddles,

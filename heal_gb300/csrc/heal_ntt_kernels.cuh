@@ -61,6 +61,11 @@ struct NttArgs {
   int canon_load;
   int force_exact;
   int bitrev;  // log2(m) when the permutation is the index's bit reversal (computed, not loaded), else 0
+  // g_decomposition on load (heal_g_decomposition_ntt, the pass that reads
+  // the source): digit limb t is digit t % gdec_power of source limb
+  // t / gdec_power (source limb stride ss[3]); 0 = off
+  int gdec_power, gdec_bits;
+  Diag *diag;
 };
 
 // row of a permutation table (load_map / store_scatter / store_gather), or
@@ -191,9 +196,40 @@ __device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
   return x;
 }
 
+// g_decomposition's capacity warning for source element (i, row, j, ts), as
+// the separate call records it (first kDiagRecords with coordinates)
+static __device__ __noinline__ void gdec_warn(const NttArgs &g, int64_t i, int64_t row, int64_t j, int64_t ts) {
+  const unsigned long long slot = atomicAdd(&g.diag->count, 1ull);
+  if (slot < (unsigned long long)kDiagRecords) {
+    DiagRecord &rec = g.diag->rec[slot];
+    rec.coord[0] = i;
+    rec.coord[1] = row;
+    rec.coord[2] = j;
+    rec.coord[3] = ts;
+    rec.ndim = 4;
+    rec.kind = 1;
+    rec.base_bits = (uint64_t)g.gdec_bits;
+    rec.power = (uint64_t)g.gdec_power;
+  }
+}
+
+// digit `d` of a loaded source value; the d == 0 load of each source element
+// also makes g_decomposition's residual check
 template <typename T>
+__device__ __forceinline__ int64_t gdec_load(const NttArgs &g, int64_t value, int d, int64_t i, int64_t row, int64_t j,
+                                             int64_t ts) {
+  if (d == 0 && gdec_residual<T>(value, (uint64_t)g.gdec_power, (uint64_t)g.gdec_bits) > 0) gdec_warn(g, i, row, j, ts);
+  return (int64_t)gdec_digit<T>(value, (uint64_t)d, (uint64_t)g.gdec_bits, (1ull << g.gdec_bits) - 1);
+}
+
+template <typename T, bool GDEC = false>
 __device__ __forceinline__ int64_t load_point(const NttArgs &g, const TileCtx &x, int s, int64_t t) {
   const int64_t v = x.row_of(g, s);
+  if (GDEC) {
+    const int64_t ts = t / g.gdec_power;
+    const int64_t raw = (int64_t)((const T *)g.src)[x.i * g.ss[0] + v * g.ss[1] + x.j * g.ss[2] + ts * g.ss[3]];
+    return gdec_load<T>(g, raw, (int)(t - ts * g.gdec_power), x.i, v, x.j, ts);
+  }
   if (g.load_map) {
     const int64_t sr = perm_row(g, g.load_map, v);
     if (sr < 0) return (int64_t)((const T *)g.old)[x.i * g.os[0] + v * g.os[1] + x.j * g.os[2] + t * g.os[3]];
@@ -274,7 +310,7 @@ __device__ __noinline__ void exact_tile(const NttArgs &g, const TileCtx &x, int6
 }
 
 // ------------------------------------------------------ generic (P < 16)
-template <typename T, bool WIDE, bool INV>
+template <typename T, bool WIDE, bool INV, bool GDEC = false>
 __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ NttArgs g) {
   typedef typename Word<WIDE>::W W;
   typedef typename Word<WIDE>::Pair Pair;
@@ -286,7 +322,7 @@ __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ 
     const int s = e >> logC, c = e & (C - 1);
     const int64_t t = x.t0 + c;
     if (t >= g.k) continue;
-    const int64_t v = load_point<T>(g, x, s, t);
+    const int64_t v = load_point<T, GDEC>(g, x, s, t);
     neg |= needs_exact<INV>(g, v, g.q[t]);
     tile[tidx(s, c, logC)] = v;
   }
@@ -510,7 +546,10 @@ __device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)
 #ifndef HEAL_NTT_MINB
 #define HEAL_NTT_MINB 2
 #endif
-template <typename T, int MODE, bool INV, int LOGP>
+// GDEC: the forward first pass of heal_g_decomposition_ntt (digits extracted
+// on load); a separate instantiation so that the plain kernels keep their
+// register allocation.
+template <typename T, int MODE, bool INV, int LOGP, bool GDEC = false>
 __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
   constexpr bool WIDE = mode_wide(MODE);
   constexpr bool LAZY = MODE != MODE_N32;
@@ -542,14 +581,20 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
       neg |= needs_exact<INV>(g, raw[e], q64);
     }
   } else {
-    const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + tq * g.ss[3]) +
+    const int64_t ts = GDEC ? tq / g.gdec_power : tq;  // source limb
+    const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + ts * g.ss[3]) +
                   x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, 0)) * g.ss[1];
     const int64_t rs = rowmul * g.ss[1];
 #pragma unroll
-    for (int e = 0; e < kPT; ++e) {
-      raw[e] = act ? (int64_t)p0[point_of<INV, LOGP, kLPT>(0, 0, e) * rs] : 0;
-      neg |= needs_exact<INV>(g, raw[e], q64);
+    for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)p0[point_of<INV, LOGP, kLPT>(0, 0, e) * rs] : 0;
+    if (GDEC && act) {
+      const int d = (int)(tq - ts * g.gdec_power);
+#pragma unroll
+      for (int e = 0; e < kPT; ++e)
+        raw[e] = gdec_load<T>(g, raw[e], d, x.i, x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, e)), x.j, ts);
     }
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) neg |= needs_exact<INV>(g, raw[e], q64);
   }
   const bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
                      (g.scale && g.minv_neg && *g.minv_neg);

@@ -18,49 +18,49 @@ static int launch_with_smem(Kern kern, const NttArgs &a, int64_t nblocks, int th
   return check_launch("ntt_pass");
 }
 
-template <typename T, int MODE, bool INV, int LOGP>
+template <typename T, int MODE, bool INV, int LOGP, bool GDEC>
 static int launch_reg(const NttArgs &a, int64_t nblocks) {
   static bool attr = false;
   const int threads = ((1 << LOGP) >> lpt_of(MODE, INV)) * a.C;
   const size_t smem = (size_t)(1 << LOGP) * a.C * sizeof(int64_t);
-  return launch_with_smem(ntt_reg_kernel<T, MODE, INV, LOGP>, a, nblocks, threads, smem, attr);
+  return launch_with_smem(ntt_reg_kernel<T, MODE, INV, LOGP, GDEC>, a, nblocks, threads, smem, attr);
 }
 
-template <typename T, bool WIDE, bool INV>
+template <typename T, bool WIDE, bool INV, bool GDEC>
 static int launch_small(const NttArgs &a, int64_t nblocks) {
   static bool attr = false;
   const size_t smem = (size_t)(1 << a.p) * a.C * sizeof(int64_t);
-  return launch_with_smem(ntt_small_kernel<T, WIDE, INV>, a, nblocks, 256, smem, attr);
+  return launch_with_smem(ntt_small_kernel<T, WIDE, INV, GDEC>, a, nblocks, 256, smem, attr);
 }
 
-template <typename T, int MODE, bool INV>
+template <typename T, int MODE, bool INV, bool GDEC>
 static int launch_typed(const NttArgs &a, int64_t nblocks) {
   switch (a.p) {
     case 3:
-      if constexpr (lpt_of(MODE, INV) <= 3) return launch_reg<T, MODE, INV, 3>(a, nblocks);
-      return launch_small<T, mode_wide(MODE), INV>(a, nblocks);
-    case 4: return launch_reg<T, MODE, INV, 4>(a, nblocks);
-    case 5: return launch_reg<T, MODE, INV, 5>(a, nblocks);
-    case 6: return launch_reg<T, MODE, INV, 6>(a, nblocks);
-    case 7: return launch_reg<T, MODE, INV, 7>(a, nblocks);
-    case 8: return launch_reg<T, MODE, INV, 8>(a, nblocks);
-    case 9: return launch_reg<T, MODE, INV, 9>(a, nblocks);
-    case 10: return launch_reg<T, MODE, INV, 10>(a, nblocks);
-    case 11: return launch_reg<T, MODE, INV, 11>(a, nblocks);
-    case 12: return launch_reg<T, MODE, INV, 12>(a, nblocks);
-    default: return launch_small<T, mode_wide(MODE), INV>(a, nblocks);
+      if constexpr (lpt_of(MODE, INV) <= 3) return launch_reg<T, MODE, INV, 3, GDEC>(a, nblocks);
+      return launch_small<T, mode_wide(MODE), INV, GDEC>(a, nblocks);
+    case 4: return launch_reg<T, MODE, INV, 4, GDEC>(a, nblocks);
+    case 5: return launch_reg<T, MODE, INV, 5, GDEC>(a, nblocks);
+    case 6: return launch_reg<T, MODE, INV, 6, GDEC>(a, nblocks);
+    case 7: return launch_reg<T, MODE, INV, 7, GDEC>(a, nblocks);
+    case 8: return launch_reg<T, MODE, INV, 8, GDEC>(a, nblocks);
+    case 9: return launch_reg<T, MODE, INV, 9, GDEC>(a, nblocks);
+    case 10: return launch_reg<T, MODE, INV, 10, GDEC>(a, nblocks);
+    case 11: return launch_reg<T, MODE, INV, 11, GDEC>(a, nblocks);
+    case 12: return launch_reg<T, MODE, INV, 12, GDEC>(a, nblocks);
+    default: return launch_small<T, mode_wide(MODE), INV, GDEC>(a, nblocks);
   }
 }
 
 // int32 tensors hold q < 2^31, so they only need the 32-bit modes
-template <typename T, bool INV>
+template <typename T, bool INV, bool GDEC = false>
 static int launch_direction_typed(const NttArgs &a, int64_t nblocks, int mode) {
   if constexpr (sizeof(T) == 8) {
-    if (mode == MODE_W64_GROW) return launch_typed<T, MODE_W64_GROW, INV>(a, nblocks);
-    if (mode == MODE_W64_LAZY) return launch_typed<T, MODE_W64_LAZY, INV>(a, nblocks);
+    if (mode == MODE_W64_GROW) return launch_typed<T, MODE_W64_GROW, INV, GDEC>(a, nblocks);
+    if (mode == MODE_W64_LAZY) return launch_typed<T, MODE_W64_LAZY, INV, GDEC>(a, nblocks);
   }
-  if (mode == MODE_N32_LAZY) return launch_typed<T, MODE_N32_LAZY, INV>(a, nblocks);
-  return launch_typed<T, MODE_N32, INV>(a, nblocks);
+  if (mode == MODE_N32_LAZY) return launch_typed<T, MODE_N32_LAZY, INV, GDEC>(a, nblocks);
+  return launch_typed<T, MODE_N32, INV, GDEC>(a, nblocks);
 }
 
 }  // namespace heal

@@ -281,21 +281,6 @@ struct GdecArgs {
   Diag *diag;
 };
 
-// Digit d of `value` after d of the reference's steps (remainder and
-// quotient of the value as uint64, quotient stored back in T), in closed
-// form.  int64: the first quotient is already non-negative, so the steps are
-// logical shifts of the uint64 image.  int32: storing uv >> bits back into
-// an int32 is an arithmetic shift of the int32 value (saturating at 31).
-template <typename T>
-__device__ __forceinline__ uint64_t gdec_digit(int64_t value, uint64_t d, uint64_t bits, uint64_t mask) {
-  const uint64_t sh = d * bits;
-  if (sizeof(T) == 4) {
-    const int32_t v = (int32_t)value >> (sh > 31 ? 31 : sh);
-    return (uint64_t)(int64_t)v & mask;
-  }
-  const uint64_t uv = (uint64_t)value;
-  return (sh >= 64 ? 0 : (uv >> sh)) & mask;
-}
 
 // Dense layout, power PW <= 8: each thread decomposes the VEC elements of one
 // 16-byte vector.  A warp stages the digits of its 32 vectors in shared

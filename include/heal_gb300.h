@@ -267,6 +267,20 @@ int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tens
 int heal_modmul_axis_sum(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
                          int64_t perm_axis, const heal_tensor *result, int64_t axis);
 
+/* The head of a keyswitch's digit transform in one call (an extension: HEAL
+ * has no such op).  Defined as the composition of HEAL's own calls
+ *   result = ntt(reshape(g_decomposition(a, power, base_bits),
+ *                        [l, m, r, k * power]), p, perm, twiddles)
+ * (example_impl/g_decomposition_impl.cpp:10-67, ntt_impl.cpp:69-116) for a of
+ * shape [l, m, r, k]: digit limb t * power + d is digit d of source limb t,
+ * p has shape [k * power] and twiddles [k * power, m].  The first pass of the
+ * transform reads a and extracts each digit as it loads, so the digit tensor
+ * is never written.  Bit-identical to the two calls, including
+ * g_decomposition's capacity warnings (printed at the next synchronisation).
+ * Errors as g_decomposition / ntt; result must have shape [l, m, r, k * power]. */
+int heal_g_decomposition_ntt(const heal_tensor *a, int64_t power, int64_t base_bits, const heal_tensor *p,
+                             const heal_tensor *perm, const heal_tensor *twiddles, const heal_tensor *result);
+
 /* The tail of a keyswitch in one pass (an extension: HEAL has no such op).
  * Defined as the composition of HEAL's own calls
  *   result = permute(axis_modsum(modmul(a, b, p), axis), perms,

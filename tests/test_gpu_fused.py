@@ -221,20 +221,22 @@ def test_post_permute_errors():
     a = np.zeros((3, 4, 2), np.int64)
     out = capi.DeviceArray.empty((4, 2), np.int64)           # result of a [3, 4, 2] reduced over axis 0
     L = capi.lib()
-    ok = up(np.tile(np.arange(4), (2, 1)).astype(np.int64))  # [result.dims[ew = 1], result.dims[pa = 0]]
-    perms = np.tile(np.arange(4), (3, 1)).astype(np.int64)   # wrong shape: [3, 4]
-    da, dp = up(a), up(p)
-    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(ok), 1, 0, capi._arg(out)) == 0
-    bad_axes = [(0, 0), (2, 0), (1, 5)]
-    for ew, pa in bad_axes:
-        assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(ok), ew, pa, capi._arg(out)) == 1
-    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(up(perms)), 1, 0, capi._arg(out)) == 1
-    oob = np.tile(np.arange(4), (2, 1)).astype(np.int64)
-    oob[1, 3] = 4
+    ok = up(np.tile(np.arange(4), (2, 1)).astype(np.int64))     # [result.dims[ew = 1], result.dims[pa = 0]]
+    wrong = up(np.tile(np.arange(4), (3, 1)).astype(np.int64))  # wrong shape: [3, 4]
+    oob_h = np.tile(np.arange(4), (2, 1)).astype(np.int64)
+    oob_h[1, 3] = 4
+    oob = up(oob_h)
+    da, dp = up(a), up(p)                                       # every operand kept alive across the calls
+    call = lambda perms, ew, pa: L.heal_modmul_axis_sum_permute(
+        capi._arg(da), capi._arg(da), capi._arg(dp), 0, capi._arg(perms), ew, pa, capi._arg(out))
+    assert call(ok, 1, 0) == 0
+    for ew, pa in [(0, 0), (2, 0), (1, 5)]:
+        assert call(ok, ew, pa) == 1
+    assert call(wrong, 1, 0) == 1
     before = out.numpy().copy()
-    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, capi._arg(up(oob)), 1, 0, capi._arg(out)) == 2
-    assert np.array_equal(out.numpy(), before)              # nothing written
-    assert L.heal_modmul_axis_sum_permute(*map(capi._arg, (da, da, dp)), 0, None, 1, 0, capi._arg(out)) == 1
+    assert call(oob, 1, 0) == 2
+    assert np.array_equal(out.numpy(), before)                  # nothing written
+    assert call(None, 1, 0) == 1
 
 
 def test_post_permute_through_lattica_hw():
@@ -256,3 +258,78 @@ def test_post_permute_through_lattica_hw():
     out2 = hw.allocate_on_hardware_64([2, 16, 1, 3])
     GB300Dispatcher().modmul_axis_sum_permute(H(a), H(b), H(p), 3, H(perms), 2, 1, out2)
     assert np.array_equal(hw.device_to_host_64(out2).numpy(), want)
+
+
+# ------------------------------------------------ heal_g_decomposition_ntt
+def gdec_ntt(a, power, bits, p_t, perm, tw_t):
+    l, m, r, k = a.shape
+    out = capi.DeviceArray.empty((l, m, r, k * power), a.dtype)
+    capi.call("heal_g_decomposition_ntt", up(a), power, bits, up(p_t), up(perm), up(tw_t), out)
+    return out.numpy()
+
+
+def gdec_then_ntt(a, power, bits, p_t, perm, tw_t):
+    wide = lambda v: np.asarray(v).astype(np.int64)
+    dig, _ = O.g_decomposition(a, power, bits)
+    l, m, r, k = a.shape
+    flat = np.ascontiguousarray(dig.reshape(l, m, r, k * power))
+    return O.ntt(wide(flat), wide(p_t), wide(perm), wide(tw_t)).astype(a.dtype)
+
+
+@pytest.mark.parametrize("dt,bound,m,power,bits", [
+    (np.int64, 2**50, 1 << 16, 3, 17),    # the keyswitch digits: two passes
+    (np.int64, 2**50, 2048, 3, 17),       # one pass
+    (np.int64, 2**40, 8192, 4, 10),
+    (np.int32, 2**30, 4096, 2, 15),
+    (np.int32, 2**31, 1 << 14, 3, 11),
+    (np.int64, 2**62, 512, 2, 31),        # lazy 64-bit ranges
+    (np.int64, 2**50, 2, 3, 17),          # the small kernel
+])
+def test_gdec_ntt_matches_composition(dt, bound, m, power, bits):
+    k = 3
+    qs = P.ntt_primes(bound, max(m, 2), k)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m, dt)
+    p_t, tw_t = np.repeat(p, power), np.repeat(tw, power, axis=0)
+    a = P.residues(m + power, (2, m, 1, k), qs, dt)
+    assert np.array_equal(gdec_ntt(a, power, bits, p_t, perm, tw_t), gdec_then_ntt(a, power, bits, p_t, perm, tw_t))
+
+
+def test_gdec_ntt_negative_values_general_perm_and_warnings(capfd):
+    m, k, power, bits = 8192, 2, 3, 17
+    qs = P.ntt_primes(2**50, m, k)
+    p, _, tw, itw, minv = P.ntt_tables(qs, m)
+    perm = np.argsort(P.splitmix64(3, m)).astype(np.int64)
+    p_t, tw_t = np.repeat(p, power), np.repeat(tw, power, axis=0)
+    a = P.residues(8, (1, m, 1, k), qs)
+    a[0, 3, 0, 1] = -5                      # digits of the uint64 image, reduced on load
+    a[0, 77, 0, 0] = (1 << 60) + 9          # above power * bits: a capacity warning
+    capi.synchronize()
+    capfd.readouterr()
+    got = gdec_ntt(a, power, bits, p_t, perm, tw_t)
+    capi.synchronize()
+    err_fused = capfd.readouterr().err
+    assert np.array_equal(got, gdec_then_ntt(a, power, bits, p_t, perm, tw_t))
+    assert "exceeds capacity with base_bits=17 and power=3" in err_fused
+    dig = capi.DeviceArray.empty((1, m, 1, k, power), np.int64)
+    capi.call("heal_g_decomposition", up(a), dig, power, bits)
+    capi.synchronize()
+    err_sep = capfd.readouterr().err
+    assert err_fused.count("exceeds") == err_sep.count("exceeds") == 2
+
+
+def test_gdec_ntt_errors():
+    qs = P.ntt_primes(2**40, 64, 2)
+    p, perm, tw, _, _ = P.ntt_tables(qs, 64)
+    a = up(P.residues(1, (1, 64, 1, 2), qs))
+    L = capi.lib()
+    dperm = up(perm)
+    dpt, dtwt, dp = up(np.repeat(p, 3)), up(np.repeat(tw, 3, axis=0)), up(p)   # kept alive across the calls
+    good = capi.DeviceArray.empty((1, 64, 1, 6), np.int64)
+    bad_shape = capi.DeviceArray.empty((1, 64, 1, 5), np.int64)
+    call = lambda out, power, bits, pt: L.heal_g_decomposition_ntt(
+        capi._arg(a), power, bits, capi._arg(pt), capi._arg(dperm), capi._arg(dtwt), capi._arg(out))
+    assert call(good, 3, 14, dpt) == 0
+    assert call(bad_shape, 3, 14, dpt) == 1
+    assert call(good, 3, 64, dpt) == 1
+    assert call(good, 0, 14, dpt) == 1
+    assert call(good, 3, 14, dp) == 1      # p must have k * power moduli
