@@ -414,6 +414,15 @@ void modmul_axis_sum_permute(const std::shared_ptr<DeviceTensor<T>> &a, const st
   check(heal_modmul_axis_sum_permute(&A, &B, &P, axis, &PM, elementwise_axis, perm_axis, &R));
 }
 
+template <typename T>
+void g_decomposition_ntt(const std::shared_ptr<DeviceTensor<T>> &a, size_t power, size_t base_bits,
+                         const std::shared_ptr<DeviceTensor<T>> &p, const std::shared_ptr<DeviceTensor<T>> &perm,
+                         const std::shared_ptr<DeviceTensor<T>> &twiddles, std::shared_ptr<DeviceTensor<T>> &result) {
+  heal_tensor A = need(a, "a"), P = need(p, "p"), PM = need(perm, "perm"), TW = need(twiddles, "twiddles"),
+              R = need(result, "result");
+  check(heal_g_decomposition_ntt(&A, (int64_t)power, (int64_t)base_bits, &P, &PM, &TW, &R));
+}
+
 void synchronize() { check(heal_synchronize()); }
 
 // ============================================================ instantiations
@@ -454,6 +463,10 @@ void synchronize() { check(heal_synchronize()); }
   template void modmul_axis_sum<T>(const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
                                    const std::shared_ptr<DeviceTensor<T>> &, const std::shared_ptr<DeviceTensor<T>> &, \
                                    int64_t, std::shared_ptr<DeviceTensor<T>> &, int64_t);                           \
+  template void g_decomposition_ntt<T>(const std::shared_ptr<DeviceTensor<T>> &, size_t, size_t,                \
+                                       const std::shared_ptr<DeviceTensor<T>> &,                                  \
+                                       const std::shared_ptr<DeviceTensor<T>> &,                                  \
+                                       const std::shared_ptr<DeviceTensor<T>> &, std::shared_ptr<DeviceTensor<T>> &); \
   template void modmul_axis_sum_permute<T>(const std::shared_ptr<DeviceTensor<T>> &,                              \
                                            const std::shared_ptr<DeviceTensor<T>> &,                              \
                                            const std::shared_ptr<DeviceTensor<T>> &, int64_t,                     \

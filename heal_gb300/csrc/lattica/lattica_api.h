@@ -127,6 +127,12 @@ template <typename T>
 void modmul_axis_sum(const std::shared_ptr<DeviceTensor<T>> &a, const std::shared_ptr<DeviceTensor<T>> &b,
                      const std::shared_ptr<DeviceTensor<T>> &p, const std::shared_ptr<DeviceTensor<T>> &perms,
                      int64_t perm_axis, std::shared_ptr<DeviceTensor<T>> &result, int64_t axis);
+// result = ntt(reshape(g_decomposition(a, power, base_bits), [l, m, r, k * power]),
+// p, perm, twiddles) in one call (an extension; see heal_g_decomposition_ntt).
+template <typename T>
+void g_decomposition_ntt(const std::shared_ptr<DeviceTensor<T>> &a, size_t power, size_t base_bits,
+                         const std::shared_ptr<DeviceTensor<T>> &p, const std::shared_ptr<DeviceTensor<T>> &perm,
+                         const std::shared_ptr<DeviceTensor<T>> &twiddles, std::shared_ptr<DeviceTensor<T>> &result);
 // result = permute(axis_modsum(modmul(a, b, p), axis), perms, elementwise_axis,
 // perm_axis) in one pass (an extension; see heal_modmul_axis_sum_permute).
 template <typename T>

@@ -4,7 +4,8 @@
 // example_impl/py_bindings.cpp:87-133 (DeviceTensor{32,64,float64};
 // <op>_{32,64,float64}), so python_execution/lattica_heal_runtime/py_wrapper.py
 // imports it unchanged.  Added: mod_*, modneg_*, moveaxis_*, get_slice_*, view_*,
-// modmul_axis_sum_*, modmul_axis_sum_permute_* and synchronize(), which HEAL's module does not export.
+// modmul_axis_sum_*, g_decomposition_ntt_*, modmul_axis_sum_permute_* and synchronize(), which HEAL's
+// module does not export.
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
 #include <torch/extension.h>
@@ -64,6 +65,8 @@ static void bind_compute(py::module_ &m, const std::string &sfx) {
   m.def(("permute_" + sfx).c_str(), &permute<T>);
   m.def(("modmul_axis_sum_" + sfx).c_str(), &modmul_axis_sum<T>, py::arg("a"), py::arg("b"), py::arg("p"),
         py::arg("perms"), py::arg("perm_axis"), py::arg("result"), py::arg("axis"));
+  m.def(("g_decomposition_ntt_" + sfx).c_str(), &g_decomposition_ntt<T>, py::arg("a"), py::arg("power"),
+        py::arg("base_bits"), py::arg("p"), py::arg("perm"), py::arg("twiddles"), py::arg("result"));
   m.def(("modmul_axis_sum_permute_" + sfx).c_str(), &modmul_axis_sum_permute<T>, py::arg("a"), py::arg("b"),
         py::arg("p"), py::arg("axis"), py::arg("perms"), py::arg("elementwise_axis"), py::arg("perm_axis"),
         py::arg("result"));

@@ -18,6 +18,7 @@ the others are:
   take_along_axis(a, perms, elementwise_axis, perm_axis, out)   HEAL permute
   modmul_axis_sum(a, b, p, axis, out, perms=None, perm_axis=0)
   modmul_axis_sum_permute(a, b, p, axis, perms, elementwise_axis, perm_axis, out)   (extension)
+  g_decomposition_ntt(a, power, base_bits, p, perm, twiddles, out)                 (extension)
   moveaxis(a, source, destination)                    a new view
   get_slice(a, *index)                                ints, slices (step > 0), Ellipsis; a new view
   new_reference(a)                                    a new view of the same tensor
@@ -112,6 +113,12 @@ class GB300Dispatcher:
 
     def modmul_axis_sum(self, a, b, p, axis, out, perms=None, perm_axis=0):
         self._f("modmul_axis_sum", a)(a, b, p, perms, perm_axis, out, axis)
+        return out
+
+    def g_decomposition_ntt(self, a, power, base_bits, p, perm, twiddles, out):
+        """ntt(reshape(g_decomposition(a, power, base_bits), [l, m, r, k * power]),
+        p, perm, twiddles) in one call (an extension op of this backend)."""
+        self._f("g_decomposition_ntt", a)(a, power, base_bits, p, perm, twiddles, out)
         return out
 
     def modmul_axis_sum_permute(self, a, b, p, axis, perms, elementwise_axis, perm_axis, out):

@@ -333,3 +333,23 @@ def test_gdec_ntt_errors():
     assert call(good, 3, 64, dpt) == 1
     assert call(good, 0, 14, dpt) == 1
     assert call(good, 3, 14, dp) == 1      # p must have k * power moduli
+
+
+def test_gdec_ntt_through_lattica_hw():
+    import torch
+    import heal_gb300
+    from heal_gb300.runtime.dispatcher import GB300Dispatcher
+    hw = heal_gb300.lattica_hw()
+    m, k, power, bits = 1024, 2, 3, 17
+    qs = P.ntt_primes(2**50, m, k)
+    p, perm, tw, _, _ = P.ntt_tables(qs, m)
+    p_t, tw_t = np.repeat(p, power), np.repeat(tw, power, axis=0)
+    a = P.residues(9, (2, m, 1, k), qs)
+    want = gdec_then_ntt(a, power, bits, p_t, perm, tw_t)
+    H = lambda x: hw.host_to_device_64(torch.from_numpy(np.ascontiguousarray(x)))
+    out = hw.allocate_on_hardware_64([2, m, 1, k * power])
+    hw.g_decomposition_ntt_64(H(a), power, bits, H(p_t), H(perm), H(tw_t), out)
+    assert np.array_equal(hw.device_to_host_64(out).numpy(), want)
+    out2 = hw.allocate_on_hardware_64([2, m, 1, k * power])
+    GB300Dispatcher().g_decomposition_ntt(H(a), power, bits, H(p_t), H(perm), H(tw_t), out2)
+    assert np.array_equal(hw.device_to_host_64(out2).numpy(), want)
