@@ -296,34 +296,45 @@ def our_arm(args):
     plans = ch.tune(cts[0]) if not args.no_tune else None
     ch.run(cts[0], outs[0])
     # two chains in flight: even steps on the library stream, odd steps on a
-    # second stream with the twin's intermediates, so that one chain's
-    # kernels fill the tails of the other's
-    ch2 = ch.twin()
-    side = torch.cuda.Stream()
+    # args.inflight chains in flight: step s runs on chain s % K, each chain
+    # with its own intermediates (twins share the resident tables and key)
+    # and its own stream (chain 0 on the library stream), so that one chain's
+    # kernels fill the tails of the others'
+    K = max(1, args.inflight)
+    chains = [ch] + [ch.twin() for _ in range(K - 1)]
+    sides = [torch.cuda.Stream() for _ in range(K - 1)]
+    ch2, side = (chains[1], sides[0]) if K > 1 else (ch.twin(), torch.cuda.Stream())  # the e2e pipeline's pair
     lib = capi.lib()
 
     def on(st):
         capi.check(lib.heal_set_stream(st.cuda_stream if st is not None else None))
 
-    def chain_step2(s):
-        if s % 2:
-            on(side)
-            ch2.run(cts[s % RING], outs[s % RING])
-            on(None)
-        else:
-            ch.run(cts[s % RING], outs[s % RING])
+    def in_flight(method):
+        def step(s):
+            c = s % K
+            if c:
+                on(sides[c - 1])
+                getattr(chains[c], method)(cts[s % RING], outs[s % RING])
+                on(None)
+            else:
+                getattr(ch, method)(cts[s % RING], outs[s % RING])
+        return step
+
+    chain_step2 = in_flight("run")
 
     def timed2(fn, steps):
         barrier()
         start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = capi.launches()
         start.record(stream)
-        side.wait_event(start)
+        for sd in sides:
+            sd.wait_event(start)
         for s in range(steps):
             fn(s)
-        joined = torch.cuda.Event()
-        joined.record(side)
-        stream.wait_event(joined)
+        for sd in sides:
+            joined = torch.cuda.Event()
+            joined.record(sd)
+            stream.wait_event(joined)
         stop.record(stream)
         stop.synchronize()
         barrier()
@@ -345,13 +356,7 @@ def our_arm(args):
     # heal_modmul_axis_sum_permute
     want0 = outs[0].numpy()
 
-    def fused_step2(s):
-        if s % 2:
-            on(side)
-            ch2.run_fused(cts[s % RING], outs[s % RING])
-            on(None)
-        else:
-            ch.run_fused(cts[s % RING], outs[s % RING])
+    fused_step2 = in_flight("run_fused")
 
     fused_step = lambda s: ch.run_fused(cts[s % RING], outs[s % RING])
     for w in range(args.warmup):
@@ -504,7 +509,8 @@ def our_arm(args):
         line = {"metric": METRIC, "value": value, "unit": "chains/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
-                "config": CONFIG, "value_one_stream": value_one,
+                "config": dict(CONFIG, streams=f"{K} chains in flight on {K} CUDA streams (value_one_stream: one "
+                                               f"stream)"), "value_one_stream": value_one,
                 "ntt_limbs_per_s": limbs_per_call * args.steps * world / (ntt_ms / 1e3),
                 "chain_hbm_frac": chain_bytes * value / world / 1e9 / hbm,
                 "roofline": {"bound": "hbm", "kernel": "heal_ntt of the 72 digit limbs ([2, 65536, 1, 72] int64)",
@@ -772,6 +778,7 @@ def main():
     ap.add_argument("--n", type=int, default=1 << 14, help="--mode request: ring degree")
     ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
     ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--inflight", type=int, default=2, help="chains in flight on their own streams")
     ap.add_argument("--probe", default="digits", choices=["digits", "cfg4", "ct-intt"])
     args = ap.parse_args()
     if args.warmup < 3:
