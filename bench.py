@@ -395,6 +395,17 @@ def our_arm(args):
     achieved = ntt_bytes / (ntt_call_ms / 1e3) / 1e9
     traffic = profile_traffic()
     chain_bytes = ch.bytes_per_chain()
+    # the integer-pipe ceiling: the same 64-bit butterfly with its operands in registers
+    import ctypes
+    peak_bf = ctypes.c_double()
+    capi.check(capi.lib().heal_ntt_butterfly_peak(256, ctypes.byref(peak_bf)))
+    ntt_bf = limbs_per_call * (N // 2) * int(np.log2(N))
+    int_roofline = {"bound": "integer pipes", "kernel": "heal_ntt of the 72 digit limbs ([2, 65536, 1, 72] int64)",
+                    "achieved": ntt_bf / (ntt_call_ms / 1e3) / 1e9, "peak": peak_bf.value / 1e9,
+                    "unit": "Gbutterfly/s", "frac": ntt_bf / (ntt_call_ms / 1e3) / peak_bf.value,
+                    "butterflies_per_call": ntt_bf,
+                    "peak_kind": "measured live: the same 64-bit growing-range butterfly with its operands in "
+                                 "registers (heal_ntt_butterfly_peak)"}
 
     # ---- per-call split of one chain step (CUDA events around each HEAL call)
     names = ["intt", "g_decomposition", "ntt", "modmul_ttt", "axis_modsum", "permute"]
@@ -518,6 +529,7 @@ def our_arm(args):
                              "frac": achieved / hbm, "algorithmic_bytes": ntt_bytes,
                              "ms_per_call": ntt_call_ms,
                              "traffic": traffic.get("bytes_per_call") if traffic else None},
+                "int_roofline": int_roofline,
                 "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                         "pipeline": "H2D and D2H on their own streams, consecutive chains alternating between two "
                                     "compute streams",

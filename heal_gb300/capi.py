@@ -81,6 +81,7 @@ SIGNATURES = {
     "heal_modmul_axis_sum": ([_P, _P, _P, _P, _I64, _P, _I64], ctypes.c_int),
     "heal_modmul_axis_sum_permute": ([_P, _P, _P, _I64, _P, _I64, _I64, _P], ctypes.c_int),
     "heal_g_decomposition_ntt": ([_P, _I64, _I64, _P, _P, _P, _P], ctypes.c_int),
+    "heal_ntt_butterfly_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "heal_ntt_set_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "heal_ntt_get_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.POINTER(ctypes.c_int),
                            ctypes.POINTER(ctypes.c_int)], ctypes.c_int),

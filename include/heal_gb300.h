@@ -245,6 +245,14 @@ int heal_ntt_autotune(int inverse, const heal_tensor *a, const heal_tensor *p, c
                       const heal_tensor *twiddles, const heal_tensor *m_inv, const heal_tensor *result, int reps,
                       int *tile_limbs, int *first_pass_log2);
 
+/* Diagnostic (no HEAL counterpart): the sustained rate, in butterflies per
+ * second, of the NTT's 64-bit growing-range forward butterfly with its
+ * operands held in registers (groups radix-8 groups of 12 butterflies per
+ * thread, 8 CTAs of 128 threads per SM): the integer-pipe ceiling that an NTT
+ * pass is compared with.  Waits for the GPU; fails while a graph is being
+ * captured. */
+int heal_ntt_butterfly_peak(int groups, double *butterflies_per_s);
+
 /* Per-row gather along perm_axis with indices perms[l, m]
  * (include/permute.h:33-40; example_impl/permute_impl.cpp:8-65). */
 int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tensor *result, int64_t elementwise_axis,

@@ -542,3 +542,13 @@ def test_two_pass_negative_values_beside_unreduced_tiles(m):
     a[1, 17, 0, 0] = 2**55                      # non-negative, above q: reduced on load
     assert np.array_equal(ntt(a, p, perm, tw), O.ntt(a, p, perm, tw))
     assert np.array_equal(intt(a, p, perm, itw, minv), O.intt(a, p, perm, itw, minv, exact=1))
+
+
+def test_butterfly_peak_diagnostic():
+    import ctypes
+    rate = ctypes.c_double()
+    L = capi.lib()
+    capi.check(L.heal_ntt_butterfly_peak(16, ctypes.byref(rate)))
+    assert 1e10 < rate.value < 1e14              # butterflies per second on one GPU
+    assert L.heal_ntt_butterfly_peak(0, ctypes.byref(rate)) == 1
+    assert L.heal_ntt_butterfly_peak(16, None) == 1
