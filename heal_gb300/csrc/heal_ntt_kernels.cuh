@@ -574,10 +574,23 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
   const int64_t rowmul = g.kind == KIND_BLOCK ? 1 : g.nsets;
   int64_t raw[kPT];
   int neg = 0;
-  if (g.load_map) {
+  if (g.load_map && !g.bitrev) {
 #pragma unroll
     for (int e = 0; e < kPT; ++e) {
       raw[e] = act ? load_point<T>(g, x, point_of<INV, LOGP, kLPT>(0, r, e), t) : 0;
+      neg |= needs_exact<INV>(g, raw[e], q64);
+    }
+  } else if (g.load_map) {
+    // gather through the bit reversal: a thread's rows are row0 | d_e with
+    // disjoint bits, and bit reversal maps disjoint bits to disjoint bits, so
+    // bitrev(row) = bitrev(row0) | bitrev(d_e): one base and a per-point offset
+    const int sh = 32 - g.bitrev;
+    const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + tq * g.ss[3]);
+    const uint32_t rb = __brev((uint32_t)x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, 0))) >> sh;
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      const uint32_t de = (uint32_t)(point_of<INV, LOGP, kLPT>(0, 0, e) * rowmul);
+      raw[e] = act ? (int64_t)p0[(int64_t)(rb | (__brev(de) >> sh)) * g.ss[1]] : 0;
       neg |= needs_exact<INV>(g, raw[e], q64);
     }
   } else {
@@ -663,6 +676,19 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
   if (!act) return;
   Pair mp;
   if (g.scale) mp = __ldg((const Pair *)g.minv_pairs + t);
+  if (g.store_scatter && g.bitrev) {  // scatter through the bit reversal (see the gather above)
+    const int sh = 32 - g.bitrev;
+    T *p1 = (T *)g.dst + (x.i * g.ds[0] + x.j * g.ds[2] + t * g.ds[3]);
+    const uint32_t rb = __brev((uint32_t)x.row_of(g, point_of<INV, LOGP, kLPT>(NSTEP - 1, r, 0))) >> sh;
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      W val = v[e];
+      if (g.scale) val = mulw<WIDE>(val, mp, q);
+      const uint32_t de = (uint32_t)(point_of<INV, LOGP, kLPT>(NSTEP - 1, 0, e) * rowmul);
+      p1[(int64_t)(rb | (__brev(de) >> sh)) * g.ds[1]] = (T)(int64_t)val;
+    }
+    return;
+  }
   if (g.store_scatter) {
 #pragma unroll
     for (int e = 0; e < kPT; ++e) {
