@@ -720,6 +720,40 @@ def request_probe(args):
     return 0
 
 
+def tail_probe(args):
+    """--mode tail: heal_modmul_axis_sum_permute alone on the keyswitch tail
+    shape (digit transforms and key [2, 65536, 1, 72] int64 -> [2, 65536, 1,
+    24]), for ncu captures; prints one JSON line with the CUDA-event time."""
+    import torch
+    import heal_gb300
+    from heal_gb300 import capi
+    from heal_gb300 import params as P
+    from heal_gb300.chain import KeyswitchChain
+    heal_gb300.build()
+    capi.check(capi.lib().heal_init(0))
+    ch = KeyswitchChain(n=N, limbs=L, digits=D, base_bits=BITS, bound_bits=BOUND)
+    ct = capi.DeviceArray.from_numpy(P.residues(5, ch.shape(), ch.qs))
+    outs = [capi.DeviceArray.empty(ch.shape(), np.int64) for _ in range(2)]
+    ch.run(ct, outs[0])
+    tail = lambda s: capi.call("heal_modmul_axis_sum_permute", ch.prod_moved, ch.key_moved, ch.dev["p"], 3,
+                               ch.dev["gal"], 2, 1, outs[s % 2])
+    for s in range(args.warmup):
+        tail(s)
+    capi.synchronize()
+    stream = torch.cuda.ExternalStream(capi.stream())
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for s in range(args.steps):
+        tail(s)
+    stop.record(stream)
+    stop.synchronize()
+    ms = start.elapsed_time(stop) / args.steps
+    nbytes = (2 * 2 * N * L * D + 2 * N * L) * 8
+    print(json.dumps({"mode": "tail", "ms_per_call": ms, "algorithmic_bytes": nbytes,
+                      "achieved_GBps": nbytes / (ms / 1e3) / 1e9}), flush=True)
+    return 0
+
+
 def ntt_probe(args):
     """--mode ntt: one batched NTT alone, for ncu captures of the pass
     kernels.  --probe digits: [batch, 65536, 1, 72] int64 under the chain's
@@ -785,7 +819,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default NTT plans instead of autotuned ones")
     ap.add_argument("--configs", default="cfg1,cfg3,cfg4,cfg5",
                     help="comma-separated configurations reported beside the headline")
-    ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request"])
+    ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request", "tail"])
     ap.add_argument("--d", type=int, default=64, help="--mode request: matrix dimension")
     ap.add_argument("--n", type=int, default=1 << 14, help="--mode request: ring degree")
     ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
@@ -797,6 +831,8 @@ def main():
         args.warmup = 3
     if args.mode == "ntt":
         return ntt_probe(args)
+    if args.mode == "tail":
+        return tail_probe(args)
     if args.mode == "request":
         return request_probe(args)
     if args.impl == "reference":
