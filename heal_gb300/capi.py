@@ -26,6 +26,12 @@ class Tensor(ctypes.Structure):
                 ("dims", ctypes.c_int64 * MAX_DIMS), ("strides", ctypes.c_int64 * MAX_DIMS)]
 
 
+class NttJob(ctypes.Structure):
+    """heal_ntt_job: one transform of a heal_ntt_batch call."""
+    _fields_ = [("a", Tensor), ("p", Tensor), ("perm", Tensor), ("twiddles", Tensor), ("m_inv", Tensor),
+                ("result", Tensor)]
+
+
 _P = ctypes.POINTER(Tensor)
 _I64, _U64, _I32, _VP, _SZ = ctypes.c_int64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t
 SIGNATURES = {
@@ -82,6 +88,7 @@ SIGNATURES = {
     "heal_modmul_axis_sum_permute": ([_P, _P, _P, _I64, _P, _I64, _I64, _P], ctypes.c_int),
     "heal_g_decomposition_ntt": ([_P, _I64, _I64, _P, _P, _P, _P], ctypes.c_int),
     "heal_ntt_butterfly_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "heal_ntt_batch": ([ctypes.c_int, ctypes.POINTER(NttJob), _I64], ctypes.c_int),
     "heal_ntt_set_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "heal_ntt_get_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.POINTER(ctypes.c_int),
                            ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
@@ -246,6 +253,23 @@ def _arg(x):
 def call(name: str, *args):
     """Calls C-ABI function `name`, passing DeviceArrays as descriptors."""
     check(getattr(lib(), name)(*[_arg(a) for a in args]))
+
+
+def ntt_jobs(jobs) -> "ctypes.Array":
+    """heal_ntt_job array from (a, p, perm, twiddles, m_inv or None, result)
+    DeviceArrays; the caller keeps the arrays alive while it is used."""
+    arr = (NttJob * max(1, len(jobs)))()
+    for i, (a, p, perm, tw, minv, res) in enumerate(jobs):
+        arr[i].a, arr[i].p, arr[i].perm, arr[i].twiddles = a.desc(), p.desc(), perm.desc(), tw.desc()
+        if minv is not None:
+            arr[i].m_inv = minv.desc()
+        arr[i].result = res.desc()
+    return arr
+
+
+def ntt_batch(inverse: bool, jobs):
+    """heal_ntt_batch over (a, p, perm, twiddles, m_inv or None, result) tuples."""
+    check(lib().heal_ntt_batch(int(bool(inverse)), ntt_jobs(jobs), len(jobs)))
 
 
 def synchronize():

@@ -33,6 +33,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -69,8 +70,69 @@ __global__ void __launch_bounds__(256) ntt_gather_kernel(const T *src, int64_t s
   }
 }
 
+int launch_ntt_batch_fwd32(const NttBatchArgs &b, int64_t nblocks, int mode, int p, int threads, size_t smem);
+int launch_ntt_batch_fwd64(const NttBatchArgs &b, int64_t nblocks, int mode, int p, int threads, size_t smem);
+int launch_ntt_batch_inv32(const NttBatchArgs &b, int64_t nblocks, int mode, int p, int threads, size_t smem);
+int launch_ntt_batch_inv64(const NttBatchArgs &b, int64_t nblocks, int mode, int p, int threads, size_t smem);
+
 // ----------------------------------------------------------- host side
+// heal_ntt_batch runs the per-transform host path (validation, tables, plans)
+// with a collector installed on the calling thread: every pass that the
+// register kernel runs is recorded instead of launched, scratch is released
+// only after the batch is enqueued, and the recorded passes are then launched
+// per kernel class, first passes before second passes.
+struct NttDeferred {
+  int phase;  // 0: first (or only) pass of its transform, 1: second pass
+  NttArgs args;
+  int64_t nblocks;
+  int mode;
+  bool is32, inv;
+};
+struct NttCollector {
+  bool validate_only = false;
+  std::vector<NttDeferred> passes;
+  size_t job_begin = 0;  // first recorded pass of the transform being prepared
+  int job_phase = 0;
+  std::vector<void *> release;
+};
+static thread_local NttCollector *t_collect = nullptr;
+
+static int launch_now(const NttArgs &a, int64_t nblocks, bool is32, int mode, bool inv);
+
+// the current transform's recorded passes, launched now (before a pass or a
+// kernel of it that cannot be recorded)
+static int flush_job(NttCollector *col) {
+  for (size_t i = col->job_begin; i < col->passes.size(); ++i) {
+    const NttDeferred &d = col->passes[i];
+    HEAL_CHECK(launch_now(d.args, d.nblocks, d.is32, d.mode, d.inv));
+  }
+  col->passes.resize(col->job_begin);
+  return HEAL_OK;
+}
+
+static void ntt_release(void *ptr) {
+  if (!ptr) return;
+  if (t_collect) t_collect->release.push_back(ptr);
+  else scratch_free(ptr);
+}
+
+static bool batchable(const NttArgs &a, int mode, bool inv) {
+  return a.gdec_power == 0 && a.p >= 3 && a.p <= kSinglePassLogMax && (a.p > 3 || lpt_of(mode, inv) <= 3);
+}
+
 static int launch_any(const NttArgs &a, int64_t nblocks, bool is32, int mode, bool inv) {
+  if (NttCollector *col = t_collect) {
+    const int phase = col->job_phase++;
+    if (batchable(a, mode, inv)) {
+      col->passes.push_back(NttDeferred{phase, a, nblocks, mode, is32, inv});
+      return HEAL_OK;
+    }
+    HEAL_CHECK(flush_job(col));
+  }
+  return launch_now(a, nblocks, is32, mode, inv);
+}
+
+static int launch_now(const NttArgs &a, int64_t nblocks, bool is32, int mode, bool inv) {
   if (inv) return is32 ? launch_ntt_pass_inv32(a, nblocks, mode) : launch_ntt_pass_inv64(a, nblocks, mode);
   if (a.gdec_power) return is32 ? launch_ntt_pass_fwd32_gdec(a, nblocks, mode) : launch_ntt_pass_fwd64_gdec(a, nblocks, mode);
   return is32 ? launch_ntt_pass_fwd32(a, nblocks, mode) : launch_ntt_pass_fwd64(a, nblocks, mode);
@@ -210,6 +272,7 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
   TwiddleTable tt, mt;
   HEAL_CHECK(twiddle_table(*tw, *p, wide, &tt));
   if (inv) HEAL_CHECK(minv_table(*minv, *p, k, wide, &mt));
+  if (t_collect && t_collect->validate_only) return HEAL_OK;
 
   heal_tensor A = *a_in;  // the source as stored (with g_decomposition: the undecomposed tensor)
   void *owned_a = nullptr;
@@ -333,6 +396,7 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
           y.dst = T2.data;
           set_strides(y.ds, T2);
           if (!rc) rc = launch_any(y, nb, is32, m2, false);
+          if (!rc && t_collect) rc = flush_job(t_collect);  // the gather reads the second pass's output
           if (!rc) {
             int64_t n = l * m * r * k;
             int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 16);
@@ -374,11 +438,51 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
       }
     }
   }
-  scratch_free(tmp);
-  scratch_free(tmp2);
-  scratch_free(owned_a);
+  ntt_release(tmp);
+  ntt_release(tmp2);
+  ntt_release(owned_a);
   if (!rc) mark_written(res->data);
   return rc;
+}
+
+
+// the recorded passes of a batch, launched per class (element type, mode,
+// direction, pass length, tile width), kNttBatch passes per launch
+static int run_collected(NttCollector &col) {
+  std::unique_ptr<NttBatchArgs> b(new NttBatchArgs);
+  for (int phase = 0; phase < 2; ++phase) {
+    std::map<std::tuple<int, int, int, int, int>, std::vector<size_t>> classes;
+    for (size_t i = 0; i < col.passes.size(); ++i) {
+      const NttDeferred &d = col.passes[i];
+      if (d.phase == phase) classes[{d.is32 ? 1 : 0, d.mode, d.inv ? 1 : 0, d.args.p, d.args.C}].push_back(i);
+    }
+    for (auto &kv : classes) {
+      const std::vector<size_t> &idx = kv.second;
+      const NttDeferred &d0 = col.passes[idx[0]];
+      const int p = d0.args.p, C = d0.args.C;
+      const int threads = ((1 << p) >> lpt_of(d0.mode, d0.inv)) * C;
+      const size_t smem = (size_t)(1 << p) * C * sizeof(int64_t);
+      for (size_t at = 0; at < idx.size();) {
+        b->n = 0;
+        b->first[0] = 0;
+        int64_t total = 0;
+        while (at < idx.size() && b->n < kNttBatch && total + col.passes[idx[at]].nblocks < 0x7FFFFFFF) {
+          const NttDeferred &d = col.passes[idx[at++]];
+          b->pass[b->n] = d.args;
+          total += d.nblocks;
+          b->first[++b->n] = (uint32_t)total;
+        }
+        if (b->n == 0) return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT batch: a transform has more than 2^31 - 1 tiles");
+        int rc;
+        if (d0.inv) rc = d0.is32 ? launch_ntt_batch_inv32(*b, total, d0.mode, p, threads, smem)
+                                 : launch_ntt_batch_inv64(*b, total, d0.mode, p, threads, smem);
+        else rc = d0.is32 ? launch_ntt_batch_fwd32(*b, total, d0.mode, p, threads, smem)
+                          : launch_ntt_batch_fwd64(*b, total, d0.mode, p, threads, smem);
+        HEAL_CHECK(rc);
+      }
+    }
+  }
+  return HEAL_OK;
 }
 
 }  // namespace heal
@@ -405,6 +509,51 @@ int heal_intt(const heal_tensor *a, const heal_tensor *p, const heal_tensor *per
   (void)log2p;
   (void)mu;
   return ntt_run(true, a, p, perm, inv_twiddles, m_inv, result);
+}
+
+
+int heal_ntt_batch(int inverse, const heal_ntt_job *jobs, int64_t count) {
+  clear_error();
+  if (count < 0 || (count > 0 && !jobs)) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_ntt_batch: no jobs");
+  if (t_collect) return set_error(HEAL_ERR_RUNTIME, "heal_ntt_batch: already running on this thread");
+  HEAL_CHECK(ensure_init());
+  const bool inv = inverse != 0;
+  // no transform may write what another reads or writes
+  for (int64_t i = 0; i < count; ++i) {
+    HEAL_CHECK(check_desc(&jobs[i].a, "a", true));
+    HEAL_CHECK(check_desc(&jobs[i].result, "result", true));
+  }
+  for (int64_t i = 0; i < count; ++i)
+    for (int64_t j = 0; j < count; ++j)
+      if (i != j && (overlaps(jobs[i].result, jobs[j].a) || overlaps(jobs[i].result, jobs[j].result)))
+        return set_error(HEAL_ERR_INVALID_ARGUMENT,
+                         "heal_ntt_batch: job " + std::to_string(i) + " writes memory job " + std::to_string(j) +
+                             " uses");
+  NttCollector col;
+  t_collect = &col;
+  struct Reset {
+    ~Reset() { t_collect = nullptr; }
+  } reset;
+  auto one = [&](int64_t i) {
+    const heal_ntt_job &j = jobs[i];
+    return ntt_run(inv, &j.a, &j.p, &j.perm, &j.twiddles, inv ? &j.m_inv : nullptr, &j.result);
+  };
+  col.validate_only = true;  // every argument error before anything is enqueued
+  for (int64_t i = 0; i < count; ++i) {
+    const int rc = one(i);
+    if (rc) return set_error(rc, "heal_ntt_batch: job " + std::to_string(i) + ": " + heal_last_error());
+  }
+  col.validate_only = false;
+  int rc = HEAL_OK;
+  for (int64_t i = 0; i < count && !rc; ++i) {
+    col.job_begin = col.passes.size();
+    col.job_phase = 0;
+    rc = one(i);
+  }
+  if (!rc) rc = run_collected(col);
+  t_collect = nullptr;
+  for (void *ptr : col.release) scratch_free(ptr);  // stream-ordered: after the launches above
+  return rc;
 }
 
 static int plan_shape(int dtype, int inverse, int64_t m, int64_t k, int *logm) {

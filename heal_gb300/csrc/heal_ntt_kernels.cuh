@@ -161,7 +161,7 @@ struct TileCtx {
   }
 };
 
-__device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
+__device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g, uint32_t block) {
   TileCtx x;
   x.P = 1 << g.p;
   x.C = g.C;
@@ -171,8 +171,8 @@ __device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
   // all), and the CTAs that share twiddle rows (same set and limbs, other
   // i, j) run within a window of ngroups_t * l * r blocks.
   int64_t tg;
-  if (g.fast_bid) {  // blockIdx.x < 2^31: divisions by invariant 32-bit divisors
-    const uint32_t bid = blockIdx.x;
+  if (g.fast_bid) {  // block < 2^31: divisions by invariant 32-bit divisors
+    const uint32_t bid = block;
     const uint32_t rest = fastdiv(bid, g.fd_groups);
     tg = bid - rest * g.fd_groups.d;
     const uint32_t rs = fastdiv(rest, g.fd_nij);
@@ -182,7 +182,7 @@ __device__ __forceinline__ TileCtx tile_ctx(const NttArgs &g) {
     x.i = ii;
     x.j = ij - ii * g.fd_r.d;
   } else {
-    const int64_t bid = blockIdx.x;
+    const int64_t bid = block;
     const int64_t nij = g.l * g.r;
     tg = bid % g.ngroups_t;
     const int64_t rest = bid / g.ngroups_t;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ 
   typedef typename Word<WIDE>::W W;
   typedef typename Word<WIDE>::Pair Pair;
   extern __shared__ __align__(16) int64_t tile[];
-  const TileCtx x = tile_ctx(g);
+  const TileCtx x = tile_ctx(g, blockIdx.x);
   const int P = x.P, C = x.C, logC = x.logC;
   int neg = 0;
   for (int e = threadIdx.x; e < P * C; e += blockDim.x) {
@@ -549,8 +549,8 @@ __device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)
 // GDEC: the forward first pass of heal_g_decomposition_ntt (digits extracted
 // on load); a separate instantiation so that the plain kernels keep their
 // register allocation.
-template <typename T, int MODE, bool INV, int LOGP, bool GDEC = false>
-__global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
+template <typename T, int MODE, bool INV, int LOGP, bool GDEC>
+__device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
   constexpr bool WIDE = mode_wide(MODE);
   constexpr bool LAZY = MODE != MODE_N32;
   constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
   typedef typename Word<WIDE>::Pair Pair;
   constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
   extern __shared__ __align__(16) int64_t tile[];
-  const TileCtx x = tile_ctx(g);
+  const TileCtx x = tile_ctx(g, block);
   const int logC = x.logC;
   const int c = threadIdx.x & (x.C - 1);
   const int r = threadIdx.x >> logC;
@@ -707,6 +707,35 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
     if (g.scale) val = mulw<WIDE>(val, mp, q);
     p1[point_of<INV, LOGP, kLPT>(NSTEP - 1, 0, e) * rsd] = (T)(int64_t)val;
   }
+}
+
+template <typename T, int MODE, bool INV, int LOGP, bool GDEC = false>
+__global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __grid_constant__ NttArgs g) {
+  ntt_reg_body<T, MODE, INV, LOGP, GDEC>(g, blockIdx.x);
+}
+
+// ---------------------------------------------------------- ragged batch
+// One launch over the passes of up to kNttBatch transforms of one kernel
+// class (element type, arithmetic mode, direction, pass length, tile width):
+// CTA b runs tile b - first[j] of pass j, j the last with first[j] <= b.
+// The arguments travel in the launch parameters, so the launch is captured
+// into a graph like any other.
+constexpr int kNttBatch = 64;  // 64 x 400-byte arguments: within the 32 KB of launch parameters
+struct NttBatchArgs {
+  int n;
+  uint32_t first[kNttBatch + 1];
+  NttArgs pass[kNttBatch];
+};
+
+template <typename T, int MODE, bool INV, int LOGP>
+__global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_batch_kernel(const __grid_constant__ NttBatchArgs b) {
+  int lo = 0, hi = b.n - 1;
+  while (lo < hi) {  // largest j with first[j] <= blockIdx.x
+    const int mid = (lo + hi + 1) >> 1;
+    if (b.first[mid] <= blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  ntt_reg_body<T, MODE, INV, LOGP, false>(b.pass[lo], blockIdx.x - b.first[lo]);
 }
 
 }  // namespace heal

@@ -52,6 +52,48 @@ static int launch_typed(const NttArgs &a, int64_t nblocks) {
   }
 }
 
+// one batched launch of register-kernel passes of one class (pass length p)
+template <typename T, int MODE, bool INV>
+static int launch_batch_typed(const NttBatchArgs &b, int64_t nblocks, int p, int threads, size_t smem) {
+  switch (p) {
+#define HEAL_NTT_BATCH_CASE(LP)                                                                          \
+  case LP:                                                                                               \
+    if constexpr (LP > 3 || lpt_of(MODE, INV) <= 3) {                                                    \
+      static bool attr = false;                                                                          \
+      if (!attr) {                                                                                       \
+        HEAL_TRY_CUDA(cudaFuncSetAttribute(ntt_reg_batch_kernel<T, MODE, INV, LP>,                       \
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));      \
+        attr = true;                                                                                     \
+      }                                                                                                  \
+      ntt_reg_batch_kernel<T, MODE, INV, LP><<<(unsigned)nblocks, threads, smem, stream()>>>(b);         \
+      return check_launch("ntt_batch_pass");                                                             \
+    }                                                                                                    \
+    break;
+    HEAL_NTT_BATCH_CASE(3)
+    HEAL_NTT_BATCH_CASE(4)
+    HEAL_NTT_BATCH_CASE(5)
+    HEAL_NTT_BATCH_CASE(6)
+    HEAL_NTT_BATCH_CASE(7)
+    HEAL_NTT_BATCH_CASE(8)
+    HEAL_NTT_BATCH_CASE(9)
+    HEAL_NTT_BATCH_CASE(10)
+    HEAL_NTT_BATCH_CASE(11)
+    HEAL_NTT_BATCH_CASE(12)
+#undef HEAL_NTT_BATCH_CASE
+  }
+  return set_error(HEAL_ERR_RUNTIME, "NTT batch: pass length without a register kernel");
+}
+
+template <typename T, bool INV>
+static int launch_batch_direction(const NttBatchArgs &b, int64_t nblocks, int mode, int p, int threads, size_t smem) {
+  if constexpr (sizeof(T) == 8) {
+    if (mode == MODE_W64_GROW) return launch_batch_typed<T, MODE_W64_GROW, INV>(b, nblocks, p, threads, smem);
+    if (mode == MODE_W64_LAZY) return launch_batch_typed<T, MODE_W64_LAZY, INV>(b, nblocks, p, threads, smem);
+  }
+  if (mode == MODE_N32_LAZY) return launch_batch_typed<T, MODE_N32_LAZY, INV>(b, nblocks, p, threads, smem);
+  return launch_batch_typed<T, MODE_N32, INV>(b, nblocks, p, threads, smem);
+}
+
 // int32 tensors hold q < 2^31, so they only need the 32-bit modes
 template <typename T, bool INV, bool GDEC = false>
 static int launch_direction_typed(const NttArgs &a, int64_t nblocks, int mode) {

@@ -275,6 +275,24 @@ int heal_permute(const heal_tensor *a, const heal_tensor *perms, const heal_tens
 int heal_modmul_axis_sum(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p, const heal_tensor *perms,
                          int64_t perm_axis, const heal_tensor *result, int64_t axis);
 
+/* A ragged batch of transforms in few launches (an extension: HEAL has no
+ * batch call).  Job i is the heal_ntt (inverse = 0) or heal_intt
+ * (inverse = 1) call with a = jobs[i].a, p, perm, twiddles (the inverse
+ * twiddles for inverse = 1), m_inv (read for inverse = 1 only) and result;
+ * the jobs may differ in every shape (ring degree, limb count, batch axes),
+ * element type and table.  Results are bit-identical to the calls one by
+ * one.  No job's result may overlap another job's input or result
+ * (invalid_argument; a job's result may alias its own input as in heal_ntt).
+ * Every job is validated, with the errors of heal_ntt / heal_intt, before
+ * anything is enqueued.  The passes of all jobs are launched grouped by
+ * kernel class (element type, arithmetic mode, pass length, tile width), up
+ * to 64 passes per launch with their arguments in the launch parameters, so
+ * the batch can be recorded in a CUDA graph like any call. */
+typedef struct heal_ntt_job {
+  heal_tensor a, p, perm, twiddles, m_inv, result;
+} heal_ntt_job;
+int heal_ntt_batch(int inverse, const heal_ntt_job *jobs, int64_t count);
+
 /* The head of a keyswitch's digit transform in one call (an extension: HEAL
  * has no such op).  Defined as the composition of HEAL's own calls
  *   result = ntt(reshape(g_decomposition(a, power, base_bits),
