@@ -604,7 +604,8 @@ def cfg4_config(args, timed):
 def ragged_config(args, timed):
     """cfg3: 256 ciphertexts of mixed ring degree and limb count, the cfg1
     chain on each; plain loop (default and autotuned NTT plans) against one
-    CUDA graph (1 branch, and 8 parallel branches: 8 to 64 measured within 10%, 8 fastest)."""
+    CUDA graph (1 branch, and 8 parallel branches: 8 to 64 measured within 10%, 8 fastest), and
+    the transforms of all ciphertexts batched (two heal_ntt_batch calls), plain and as one graph."""
     import hashlib
     from heal_gb300 import capi
     from heal_gb300.configs import Cfg3
@@ -632,8 +633,21 @@ def ragged_config(args, timed):
         ms, launches = timed(lambda s: g.launch(), steps)
         res[nb] = (ms / steps, launches / steps, same)
         del g
+    # the transforms of all 256 ciphertexts in two heal_ntt_batch calls
+    for a in c3.AS:
+        capi.call("heal_copy_strided", capi.DeviceArray.from_numpy(np.zeros(a.shape, np.int64)), a)
+    c3.run_batched()
+    batched_same = digest() == want
+    ms_bplain, l_bplain = timed(lambda s: c3.run_batched(), steps)
+    gb = c3.graph_batched(8)
+    for a in c3.AS:
+        capi.call("heal_copy_strided", capi.DeviceArray.from_numpy(np.zeros(a.shape, np.int64)), a)
+    gb.launch()
+    batched_same = batched_same and digest() == want
+    ms_bgraph, l_bgraph = timed(lambda s: gb.launch(), steps)
+    del gb
     round_trip = all(np.array_equal(c3.RA[i].numpy(), c3.A[i].numpy()) for i in range(len(c3.specs)))
-    best = min(res[1][0], res[8][0])
+    best = min(res[1][0], res[8][0], ms_bgraph / steps)
     shapes = sorted(plans)
     return {"workload": "256 ciphertexts [2, N, 1, L] int64, N in 2^12..2^16, L uniform in 2..32, 30-bit primes; "
                         "ntt(A), ntt(B), intt(ntt(A)), modmul, axis_modsum per ciphertext (1280 calls per step)",
@@ -642,6 +656,8 @@ def ragged_config(args, timed):
             "step_ms_plain_default_plans": ms_default / steps,
             "step_ms_plain_tuned_plans": ms_tuned / steps,
             "step_ms_graph_1_branch": res[1][0], "step_ms_graph_8_branches": res[8][0],
+            "step_ms_batched_plain": ms_bplain / steps, "step_ms_batched_graph_8_branches": ms_bgraph / steps,
+            "batched_launches_per_step": l_bgraph / steps, "batched_equals_loop": batched_same,
             "graph_speedup_vs_plain": (ms_default / steps) / best,
             "ciphertexts_per_s": len(c3.specs) / (best / 1e3),
             "transform_limbs_per_s": c3.transform_limbs() / (best / 1e3),

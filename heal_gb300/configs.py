@@ -129,6 +129,57 @@ class Cfg3:
         for i in range(len(self.specs)):
             self.chain(i)
 
+    # ---- the same chain with the transforms of all ciphertexts batched
+    def _batch_jobs(self):
+        if not hasattr(self, "_jobs"):
+            fwd = []
+            for i in range(len(self.specs)):
+                v = self.views[i]
+                fwd.append((self.A[i], v["p"], v["perm"], v["tw"], None, self.NA[i]))
+                fwd.append((self.B[i], v["p"], v["perm"], v["tw"], None, self.NB[i]))
+            inv = [(self.NA[i], v["p"], v["perm"], v["itw"], v["minv"], self.RA[i])
+                   for i, v in enumerate(self.views)]
+            self._jobs = (capi.ntt_jobs(fwd), len(fwd), capi.ntt_jobs(inv), len(inv))
+        return self._jobs
+
+    def transforms_batched(self):
+        """ntt(A_i) and ntt(B_i) of every ciphertext as one heal_ntt_batch,
+        then intt(ntt(A_i)) of every ciphertext as another."""
+        fwd, nf, inv, ni = self._batch_jobs()
+        lib = capi.lib()
+        capi.check(lib.heal_ntt_batch(0, fwd, nf))
+        capi.check(lib.heal_ntt_batch(1, inv, ni))
+
+    def elementwise(self, i: int):
+        v = self.views[i]
+        capi.call("heal_modmul_ttt", self.NA[i], self.NB[i], v["p"], self.PR[i])
+        capi.call("heal_axis_modsum", self.PR[i], v["p"], self.AS[i], 0)
+
+    def run_batched(self):
+        """The chain of every ciphertext with its 768 transforms in two
+        batched calls; modmul and axis_modsum per ciphertext.  Bit-identical
+        to run()."""
+        self.transforms_batched()
+        for i in range(len(self.specs)):
+            self.elementwise(i)
+
+    def graph_batched(self, branches: int = 8) -> capi.Graph:
+        """run_batched as one CUDA graph: the two transform batches, then the
+        per-ciphertext modmul and axis_modsum spread over `branches` parallel
+        branches (forked after the batches, which they read)."""
+        lib = capi.lib()
+        plan = self.schedule(branches)
+
+        def rec():
+            self.transforms_batched()
+            capi.check(lib.heal_graph_fork(branches))
+            for b, cts in enumerate(plan):
+                capi.check(lib.heal_graph_branch(b))
+                for i in cts:
+                    self.elementwise(i)
+            capi.check(lib.heal_graph_branch(-1))
+        return capi.Graph(rec)
+
     def schedule(self, branches: int) -> list[list[int]]:
         """Ciphertexts per branch: largest first onto the least loaded branch."""
         load, out = [0] * branches, [[] for _ in range(branches)]

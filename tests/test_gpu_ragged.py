@@ -70,6 +70,26 @@ def test_ragged_graph_with_branches_vs_oracle(ragged, branches):
         check_against_oracle(c, i)
 
 
+def test_ragged_batched_vs_oracle(ragged):
+    """The transforms of every ciphertext in two heal_ntt_batch calls, plain
+    and as a graph with branches, against the oracle."""
+    c = ragged
+    c.run()
+    for lst in (c.NA, c.NB, c.RA, c.PR, c.AS):
+        for arr in lst:
+            zero(arr)
+    c.run_batched()
+    for i in range(len(c.specs)):
+        check_against_oracle(c, i)
+    g = c.graph_batched(3)
+    for lst in (c.NA, c.NB, c.RA, c.PR, c.AS):
+        for arr in lst:
+            zero(arr)
+    g.launch()
+    for i in range(len(c.specs)):
+        check_against_oracle(c, i)
+
+
 def test_schedule_balances_branches(ragged):
     plan = ragged.schedule(4)
     assert sorted(i for b in plan for i in b) == list(range(len(ragged.specs)))
