@@ -544,11 +544,20 @@ int heal_ntt_batch(int inverse, const heal_ntt_job *jobs, int64_t count) {
     if (rc) return set_error(rc, "heal_ntt_batch: job " + std::to_string(i) + ": " + heal_last_error());
   }
   col.validate_only = false;
+  // The recorded passes are launched every kBatchFlush jobs: a job touches at
+  // most 5 cached tables, so the tables of the recorded passes stay among the
+  // cache's most recent entries and none is evicted (its buffer freed) before
+  // the passes that read it are enqueued.
+  constexpr int64_t kBatchFlush = 512;
   int rc = HEAL_OK;
   for (int64_t i = 0; i < count && !rc; ++i) {
     col.job_begin = col.passes.size();
     col.job_phase = 0;
     rc = one(i);
+    if (!rc && (i + 1) % kBatchFlush == 0) {
+      rc = run_collected(col);
+      col.passes.clear();
+    }
   }
   if (!rc) rc = run_collected(col);
   t_collect = nullptr;

@@ -123,3 +123,17 @@ def test_batch_in_a_graph(inverse):
     g.launch()
     for d, w in zip(fresh, want):
         assert np.array_equal(d[5].numpy(), w)
+
+
+def test_batch_larger_than_one_flush():
+    """More than 512 jobs: the recorded passes are launched in several groups."""
+    shapes = [(1, 64 << (i % 4), 1, 1 + i % 3, np.int64, 2**50) for i in range(1100)]
+    host, dev = make_jobs(13, shapes[:8], False)
+    jobs = []
+    for i in range(len(shapes)):
+        a, p, perm, tw, _, _ = dev[i % 8]
+        jobs.append((a, p, perm, tw, None, capi.DeviceArray.empty(a.shape, np.int64)))
+    capi.ntt_batch(False, jobs)
+    want = one_by_one(False, dev[:8])
+    for i, j in enumerate(jobs):
+        assert np.array_equal(j[5].numpy(), want[i % 8]), i
