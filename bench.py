@@ -598,7 +598,45 @@ def cfg4_config(args, timed):
     per = ms4 / st4
     return {"workload": "ntt on [64, 65536, 1, 32] int32, 31-bit primes, radix-8 Shoup butterflies on the integer "
                         "pipes", "ntt_ms": per, "intt_ms": ms4i / st4, "limbs_per_s": c4.limbs() / (per / 1e3),
-            "hbm_frac": c4.bytes_per_call() / (per / 1e3) / 1e9 / hbm, "round_trip_exact": round_trip}
+            "hbm_frac": c4.bytes_per_call() / (per / 1e3) / 1e9 / hbm, "round_trip_exact": round_trip,
+            "tensor_core_floor": tensor_floor(c4.limbs(), per)}
+
+
+def tensor_floor(limb_polys: int, cuda_core_ms: float) -> dict:
+    """The exact tensor-core alternative for cfg4, bounded from below by the
+    GEMM work alone: a four-step 256 x 256 NTT of 31-bit residues whose
+    radix-256 DFTs run as byte-plane GEMMs (4 x 4 planes, exact with INT32 or
+    FP32 accumulation over K = 256) costs 2 flops x 2 passes x 16 planes x
+    256^3 MACs per limb-polynomial.  The dense INT8 rate is measured here with
+    torch._int_mm (cuBLASLt) on 8192^3, the bf16 rate with torch.matmul; twiddle
+    products, recombination and reduction mod q come on top of the floor."""
+    import torch
+    ops = 2 * 2 * 16 * 256 ** 3 * limb_polys
+    n = 8192
+    a8 = torch.randint(-64, 64, (n, n), dtype=torch.int8, device="cuda")
+    b8 = torch.randint(-64, 64, (n, n), dtype=torch.int8, device="cuda")
+    a16, b16 = a8.to(torch.bfloat16), b8.to(torch.bfloat16)
+
+    def rate(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = float("inf")
+        for _ in range(reps):
+            st.record()
+            fn()
+            en.record()
+            en.synchronize()
+            best = min(best, st.elapsed_time(en))
+        return 2 * n ** 3 / (best / 1e3)
+
+    i8 = rate(lambda: torch._int_mm(a8, b8))
+    bf = rate(lambda: torch.matmul(a16, b16))
+    del a8, b8, a16, b16
+    return {"gemm_flop_per_call": ops, "int8_dense_tops_measured": i8 / 1e12, "bf16_dense_tflops_measured": bf / 1e12,
+            "int8_floor_ms": ops / i8 * 1e3, "bf16_floor_ms": ops / bf * 1e3, "cuda_core_ntt_ms": cuda_core_ms,
+            "method": "GEMM work only (4 x 4 byte planes, 2 passes of 256-point DFTs) at the rates measured in this "
+                      "run; a tensor-core NTT is worth building only if its floor is well below the CUDA-core time"}
 
 
 def ragged_config(args, timed):
