@@ -373,7 +373,21 @@ def our_arm(args):
         tail(w)
     tail_ms, _ = timed(tail, args.steps)
     value_f = whole_job_rate(args.steps, world, ms_f2)
+    # the fused chain on 8 ciphertexts per call (one [16, N, 1, L] tensor, the key broadcast)
+    KB = 8
+    kb = ch.batched(KB)
+    kcts = [capi.DeviceArray.from_numpy(np.concatenate([cts_host[(j + i) % RING] for i in range(KB)], axis=0))
+            for j in range(2)]
+    kouts = [capi.DeviceArray.empty(kb.shape(), np.int64) for _ in range(2)]
+    kb.run(kcts[0], kouts[0])
+    assert np.array_equal(kouts[0].numpy()[:2], want0), "batched fused chain differs from the per-call chain"
+    for w in range(args.warmup):
+        kb.run(kcts[w % 2], kouts[w % 2])
+    ksteps = max(5, args.steps // KB)
+    ms_kb, _ = timed(lambda s: kb.run(kcts[s % 2], kouts[s % 2]), ksteps)
+    batched_rate = whole_job_rate(ksteps * KB, world, ms_kb)
     fused_chain = {"value": value_f, "unit": "chains/s", "value_one_stream": whole_job_rate(args.steps, world, ms_f1),
+                   "batched_8_per_call": batched_rate,
                    "vs_per_call": value_f / value, "calls_per_step": 3, "launches_per_step": launches_f / args.steps,
                    "tail_ms_per_call": tail_ms / args.steps,
                    "tail_achieved_GBps": (2 * 2 * N * L * D + 2 * N * L) * 8 / (tail_ms / args.steps / 1e3) / 1e9,

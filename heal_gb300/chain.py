@@ -109,6 +109,10 @@ class KeyswitchChain:
         dg = ct * self.D
         return (2 * ct) + (ct + dg) + (2 * dg + ct)
 
+    def batched(self, count: int) -> "KeyswitchBatch":
+        """A fused chain over `count` ciphertexts at once (same tables and key)."""
+        return KeyswitchBatch(self, count)
+
     # ---- algorithmic bytes (reads + writes of the six calls, tables excluded)
     def bytes_per_chain(self) -> int:
         e = self.dtype.itemsize
@@ -118,6 +122,40 @@ class KeyswitchChain:
 
     def ntt_limbs_per_chain(self) -> int:
         return 2 * self.L + 2 * self.L * self.D
+
+
+class KeyswitchBatch:
+    """The fused chain (KeyswitchChain.run_fused) on `count` ciphertexts in the
+    same three calls: the ciphertexts are one tensor [2 * count, N, 1, L]
+    (ciphertext-major), the key [2, N, 1, L * D] is broadcast over them in
+    the tail, and every kernel runs count times the tiles.  Each output
+    [2, N, 1, L] slice equals the single chain's output for its ciphertext."""
+
+    def __init__(self, chain: KeyswitchChain, count: int):
+        self.ch, self.count = chain, count
+        n, L, D = chain.n, chain.L, chain.D
+        E = capi.DeviceArray.empty
+        B = 2 * count
+        self.x = E((B, n, 1, L), chain.dtype, zero=False)
+        self.dn = E((B, n, 1, L * D), chain.dtype, zero=False)
+        # [count, 2, N, 1, D, L] views of the digit transforms and of the key
+        self.dn_moved = self.dn.reshape((count, 2, n, 1, L, D)).moveaxis(5, 4)
+        self.key_moved = chain.dev["key"].reshape((1, 2, n, 1, L, D)).moveaxis(5, 4)
+        # the Galois rows per ciphertext component: the permutation's elementwise
+        # axis is the component axis (2 rows, the same map), so the result view
+        # merges to 4 axes
+        self.gal2 = capi.DeviceArray.from_numpy(np.repeat(chain.host["gal"], 2, axis=0))
+
+    def shape(self):
+        return (2 * self.count, self.ch.n, 1, self.ch.L)
+
+    def run(self, cts: capi.DeviceArray, out: capi.DeviceArray):
+        """cts and out: [2 * count, N, 1, L]."""
+        ch, d = self.ch, self.ch.dev
+        capi.call("heal_intt", cts, d["p"], d["perm"], d["itw"], d["minv"], None, None, self.x)
+        capi.call("heal_g_decomposition_ntt", self.x, ch.D, ch.bits, d["p_t"], d["perm"], d["tw_t"], self.dn)
+        o = out.reshape((self.count, 2, ch.n, 1, ch.L))
+        capi.call("heal_modmul_axis_sum_permute", self.dn_moved, self.key_moved, d["p"], 4, self.gal2, 1, 2, o)
 
 
 def oracle_chain(ch_host: dict, ct: np.ndarray, digits: int, base_bits: int, limb_idx=None):

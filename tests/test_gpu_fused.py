@@ -353,3 +353,22 @@ def test_gdec_ntt_through_lattica_hw():
     out2 = hw.allocate_on_hardware_64([2, m, 1, k * power])
     GB300Dispatcher().g_decomposition_ntt(H(a), power, bits, H(p_t), H(perm), H(tw_t), out2)
     assert np.array_equal(hw.device_to_host_64(out2).numpy(), want)
+
+
+def test_keyswitch_batch_equals_single_chains():
+    from heal_gb300.chain import KeyswitchChain
+    ch = KeyswitchChain(n=1024, limbs=4, digits=3, base_bits=17, bound_bits=50)
+    count = 3
+    host = [P.residues(50 + i, ch.shape(), ch.qs) for i in range(count)]
+    want = []
+    for h in host:
+        out = capi.DeviceArray.empty(ch.shape(), np.int64)
+        ch.run(capi.DeviceArray.from_numpy(h), out)
+        want.append(out.numpy())
+    kb = ch.batched(count)
+    cts = capi.DeviceArray.from_numpy(np.concatenate(host, axis=0))
+    out = capi.DeviceArray.empty(kb.shape(), np.int64)
+    kb.run(cts, out)
+    got = out.numpy()
+    for i in range(count):
+        assert np.array_equal(got[2 * i:2 * i + 2], want[i]), i
