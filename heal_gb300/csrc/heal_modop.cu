@@ -121,8 +121,17 @@ struct VecOf {
 // two vectors per iteration.  With HOIST the grid stride is a multiple of
 // the modulus period (`last`), so every thread keeps the same moduli for its
 // whole run and loads their constants once.
+// Grid: 8 CTAs of 256 threads per SM, except for the 64-bit multiplication.
+// Its reduction took 66 registers (3 resident CTAs per SM against a grid of
+// 8, so the last of 2.7 waves ran a third empty); its own entry kernel
+// (modop_dense_mul64_kernel) is held to 64 registers by its launch bound, 4
+// resident CTAs, and its grid is exactly 4 per SM.
+template <typename T, int OP>
+constexpr bool dense_wide_mul() { return OP == OP_MUL && sizeof(T) == 8; }
+template <typename T, int OP>
+constexpr int dense_blocks_per_sm() { return dense_wide_mul<T, OP>() ? 4 : 8; }
 template <typename T, int OP, int VEC, bool HOIST>
-__global__ void __launch_bounds__(256) modop_dense_kernel(const __grid_constant__ ModopArgs g) {
+__device__ __forceinline__ void modop_dense_body(const ModopArgs &g) {
   typedef typename VecOf<T>::type V;
   typedef typename MGOf<T>::type M;
   const T *A = (const T *)g.ap;
@@ -213,6 +222,17 @@ __global__ void __launch_bounds__(256) modop_dense_kernel(const __grid_constant_
     int64_t b = B ? (int64_t)B[i] : g.bs;
     R[i] = elem_op<T, OP>((int64_t)A[i], b, q_of<T>(g, c), c, g.diag);
   }
+}
+
+template <typename T, int OP, int VEC, bool HOIST>
+__global__ void __launch_bounds__(256) modop_dense_kernel(const __grid_constant__ ModopArgs g) {
+  modop_dense_body<T, OP, VEC, HOIST>(g);
+}
+
+template <int VEC, bool HOIST>
+__global__ void __launch_bounds__(256, dense_blocks_per_sm<int64_t, OP_MUL>())
+    modop_dense_mul64_kernel(const __grid_constant__ ModopArgs g) {
+  modop_dense_body<int64_t, OP_MUL, VEC, HOIST>(g);
 }
 
 // ---------------------------------------------------- general kernel
@@ -488,10 +508,17 @@ static void launch_dense(ModopArgs &g, cudaStream_t s, int64_t want_blocks) {
   const int64_t vecs = (g.n / VEC + 1) / 2 + 1;  // two vectors per thread per iteration
   const int64_t want = std::max<int64_t>(1, std::min<int64_t>(want_blocks, (vecs + 255) / 256));
   const int64_t hb = g.p_per_last ? hoist_blocks(g.last, VEC, want_blocks) : want;
-  if (hb > 0)
-    modop_dense_kernel<T, OP, VEC, true><<<(unsigned)hb, 256, 0, s>>>(g);
-  else
-    modop_dense_kernel<T, OP, VEC, false><<<(unsigned)want, 256, 0, s>>>(g);
+  if constexpr (dense_wide_mul<T, OP>()) {
+    if (hb > 0)
+      modop_dense_mul64_kernel<VEC, true><<<(unsigned)hb, 256, 0, s>>>(g);
+    else
+      modop_dense_mul64_kernel<VEC, false><<<(unsigned)want, 256, 0, s>>>(g);
+  } else {
+    if (hb > 0)
+      modop_dense_kernel<T, OP, VEC, true><<<(unsigned)hb, 256, 0, s>>>(g);
+    else
+      modop_dense_kernel<T, OP, VEC, false><<<(unsigned)want, 256, 0, s>>>(g);
+  }
 }
 
 enum Kind { KIND_GENERAL = 0, KIND_DENSE = 1, KIND_VEC = 2 };
@@ -508,7 +535,7 @@ static int launch(ModopArgs &g, int kind) {
       modop_vec_kernel<T, OP, VEC, int64_t><<<grid, 256, 0, s>>>(g);
   } else if (kind == KIND_DENSE) {
     bool aligned = ((uintptr_t)g.ap % 16 == 0) && ((uintptr_t)g.rp % 16 == 0) && (!g.bp || (uintptr_t)g.bp % 16 == 0);
-    const int64_t want = (int64_t)std::max(device_sm_count(), 1) * 8;
+    const int64_t want = (int64_t)std::max(device_sm_count(), 1) * dense_blocks_per_sm<T, OP>();
     if (aligned)
       launch_dense<T, OP, 16 / sizeof(T)>(g, s, want);
     else
@@ -717,7 +744,7 @@ static int noalloc_launch(ModopArgs &g, bool dense, cudaStream_t s, int sms) {
   if (dense) {
     const int vec = 16 / sizeof(T);
     bool aligned = ((uintptr_t)g.ap % 16 == 0) && ((uintptr_t)g.rp % 16 == 0) && ((uintptr_t)g.bp % 16 == 0);
-    const int64_t want = (int64_t)std::max(sms, 1) * 8;
+    const int64_t want = (int64_t)std::max(sms, 1) * dense_blocks_per_sm<T, OP_MUL>();
     (void)vec;
     if (aligned)
       launch_dense<T, OP_MUL, 16 / sizeof(T)>(g, s, want);
