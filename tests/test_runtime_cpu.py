@@ -135,3 +135,64 @@ def test_generator_reproduces_the_committed_transcripts(tmp_path):
     for path in GOLD:
         new = R.load_transcript_from_json(str(tmp_path / os.path.basename(path)))
         assert flat(new) == flat(R.load_transcript_from_json(path)), path
+
+
+def _reference_runtime():
+    if not os.path.isdir(REF_RUNTIME):
+        pytest.skip("HEAL's runtime sources are not on this machine")
+    sys.path.insert(0, REF_RUNTIME)
+    try:
+        return tuple(importlib.import_module(f"lattica_heal_runtime.{m}")
+                     for m in ("runtime", "device_interface", "serialization"))
+    finally:
+        sys.path.remove(REF_RUNTIME)
+
+
+class _Token:
+    def __init__(self, n):
+        self.n = n
+
+
+class Recorder:
+    """Stands in for a device: records every call with its arguments resolved
+    (a device tensor as the index of the call that produced it) and returns a
+    new token per call."""
+
+    def __init__(self):
+        self.calls = []
+
+    def _norm(self, v):
+        if isinstance(v, _Token):
+            return ("dev", v.n)
+        if isinstance(v, torch.Tensor):
+            return ("host", str(v.dtype), tuple(v.shape), v.contiguous().numpy().tobytes())
+        if isinstance(v, (tuple, list)):
+            return tuple(self._norm(x) for x in v)
+        if isinstance(v, slice):
+            return ("slice", v.start, v.stop, v.step)
+        return ("v", repr(v))
+
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+
+        def call(*args, **kwargs):
+            self.calls.append((name, self._norm(args), self._norm(tuple(sorted(kwargs.items())))))
+            return _Token(len(self.calls) - 1)
+        return call
+
+
+@pytest.mark.parametrize("path", GOLD, ids=os.path.basename)
+def test_heal_runtime_makes_the_calls_our_executor_makes(path):
+    """HEAL's own run_transcript, through HEAL's DeviceDispatcher, issues the
+    same device calls with the same arguments as this repository's executor,
+    which the GPU tests run on GB300Dispatcher."""
+    runtime, device_interface, serialization = _reference_runtime()
+    theirs = Recorder()
+    runtime.run_transcript(device_interface.DeviceDispatcher(theirs),
+                           serialization.load_transcript_from_json(path).transcript, verify=False)
+    ours = Recorder()
+    run_transcript(ours, R.load_transcript_from_json(path), verify=False)
+    ours_calls = [c for c in ours.calls if c[0] != "synchronize"]
+    assert len(theirs.calls) > 10
+    assert theirs.calls == ours_calls
