@@ -558,29 +558,30 @@ def our_arm(args):
 
 
 def other_configs(args, timed, stream):
-    """The other configurations, timed like the headline: cfg1 (plain and as
-    one CUDA graph), cfg4, cfg3 (ragged batch) and cfg5 (serving loop)."""
+    """The other workloads, timed like the headline: the N = 4096 round-trip
+    chain (plain and as one CUDA graph), the int32 NTT of [64, 65536, 1, 32],
+    the ragged batch of 256 ciphertexts and the serving loop."""
     out = {}
     want = set(args.configs.split(","))
-    if "cfg1" in want:
-        out["cfg1"] = cfg1_config(args, timed)
-    if "cfg4" in want:
-        out["cfg4"] = cfg4_config(args, timed)
-    if "cfg3" in want:
-        out["cfg3"] = ragged_config(args, timed)
-    if "cfg5" in want:
-        out["cfg5"] = serving_config(args)
+    if "roundtrip" in want:
+        out["roundtrip_n4096"] = roundtrip_config(args, timed)
+    if "int32_ntt" in want:
+        out["int32_ntt_n65536"] = int32_ntt_config(args, timed)
+    if "ragged" in want:
+        out["ragged_256"] = ragged_config(args, timed)
+    if "serving" in want:
+        out["serving"] = serving_config(args)
     return out
 
 
-def cfg1_config(args, timed):
+def roundtrip_config(args, timed):
     import hashlib
     from heal_gb300 import capi
-    from heal_gb300.configs import Cfg1
-    c1 = Cfg1()
+    from heal_gb300.configs import RoundTripChain
+    c1 = RoundTripChain()
     c1.run()
     with open(os.path.join(ROOT, "tests", "golden", "golden_hash.json")) as f:
-        gh = json.load(f)["cfg1"]
+        gh = json.load(f)["roundtrip_n4096"]
     sha = lambda a: hashlib.sha256(np.ascontiguousarray(a.numpy()).tobytes()).hexdigest()
     exact = sha(c1.NA) == gh["ntt_a"] and sha(c1.AS) == gh["axis_modsum"] and sha(c1.RA) == gh["intt_ntt_a"]
     steps = max(args.steps, 50)
@@ -599,9 +600,9 @@ def cfg1_config(args, timed):
             "launches_per_step": l_graph / steps}
 
 
-def cfg4_config(args, timed):
-    from heal_gb300.configs import Cfg4
-    c4 = Cfg4()
+def int32_ntt_config(args, timed):
+    from heal_gb300.configs import Int32Ntt
+    c4 = Int32Ntt()
     c4.ntt()
     c4.intt()
     round_trip = bool(np.array_equal(c4.Z.numpy()[:2], c4.host_x[:2]))
@@ -617,7 +618,7 @@ def cfg4_config(args, timed):
 
 
 def tensor_floor(limb_polys: int, cuda_core_ms: float) -> dict:
-    """The exact tensor-core alternative for cfg4, bounded from below by the
+    """The exact tensor-core alternative for the int32 NTT, bounded from below by the
     GEMM work alone: a four-step 256 x 256 NTT of 31-bit residues whose
     radix-256 DFTs run as byte-plane GEMMs (4 x 4 planes, exact with INT32 or
     FP32 accumulation over K = 256) costs 2 flops x 2 passes x 16 planes x
@@ -654,16 +655,16 @@ def tensor_floor(limb_polys: int, cuda_core_ms: float) -> dict:
 
 
 def ragged_config(args, timed):
-    """cfg3: 256 ciphertexts of mixed ring degree and limb count, the cfg1
+    """Ragged batch: 256 ciphertexts of mixed ring degree and limb count, the round-trip
     chain on each; plain loop (default and autotuned NTT plans) against one
     CUDA graph (1 branch, and 8 parallel branches: 8 to 64 measured within 10%, 8 fastest), and
     the transforms of all ciphertexts batched (two heal_ntt_batch calls), plain and as one graph."""
     import hashlib
     from heal_gb300 import capi
-    from heal_gb300.configs import Cfg3
+    from heal_gb300.configs import RaggedBatch
     hbm, _ = peaks()
     t0 = time.time()
-    c3 = Cfg3()
+    c3 = RaggedBatch()
     setup_s = time.time() - t0
     c3.run()                                           # caches every table
     steps = max(5, args.steps // 40)
@@ -722,7 +723,7 @@ def ragged_config(args, timed):
 
 
 def serving_config(args, count: int = 4000, rate: float = 2000.0):
-    """cfg5: Poisson arrivals of ciphertext x plaintext-matrix products
+    """Serving loop: Poisson arrivals of ciphertext x plaintext-matrix products
     admitted by HBM footprint; served with the three HEAL calls (permute
     rotations, modmul, axis_modsum) and with the fused modmul_axis_sum."""
     out = {"workload": f"{count} Poisson arrivals at {rate:.0f}/s of ct[2][N][L] x (d x d plaintext matrix): "
@@ -825,7 +826,7 @@ def tail_probe(args):
 def ntt_probe(args):
     """--mode ntt: one batched NTT alone, for ncu captures of the pass
     kernels.  --probe digits: [batch, 65536, 1, 72] int64 under the chain's
-    50-bit primes tiled 3x (the digit tensor of batch/2 chains); --probe cfg4:
+    50-bit primes tiled 3x (the digit tensor of batch/2 chains); --probe int32:
     [batch, 65536, 1, 32] int32 under 31-bit primes; --probe ct-intt: the INTT
     of [batch, 65536, 1, 24] int64 (the chain's ciphertext).  Prints one JSON
     line with the CUDA-event time per call."""
@@ -837,7 +838,7 @@ def ntt_probe(args):
     capi.check(capi.lib().heal_init(0))
     stream = torch.cuda.ExternalStream(capi.stream())
     inverse = args.probe == "ct-intt"
-    if args.probe == "cfg4":
+    if args.probe == "int32":
         dt, k, qs = np.int32, 32, P.ntt_primes(1 << 31, N, 32)
         p_t, perm, tw_t, itw, minv = P.ntt_tables(qs, N, dt)
     elif inverse:
@@ -885,7 +886,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default NTT plans instead of autotuned ones")
-    ap.add_argument("--configs", default="cfg1,cfg3,cfg4,cfg5",
+    ap.add_argument("--configs", default="roundtrip,ragged,int32_ntt,serving",
                     help="comma-separated configurations reported beside the headline")
     ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request", "tail"])
     ap.add_argument("--d", type=int, default=64, help="--mode request: matrix dimension")
@@ -893,7 +894,7 @@ def main():
     ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--inflight", type=int, default=2, help="chains in flight on their own streams")
-    ap.add_argument("--probe", default="digits", choices=["digits", "cfg4", "ct-intt"])
+    ap.add_argument("--probe", default="digits", choices=["digits", "int32", "ct-intt"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1,13 +1,15 @@
 """Workloads of the benchmark configurations, built through the C ABI.
 
-cfg1  plain batched NTT -> INTT round trip: N = 2^12, the 4 largest primes
+RoundTripChain  plain batched NTT -> INTT round trip: N = 2^12, the 4 largest primes
       q < 2^30 with q = 1 (mod 2N), a batch of 8 polynomials [8, N, 1, 4]
       int64; then modmul of two NTT-domain tensors and axis_modsum over the
       batch axis.  Five HEAL calls per step, small enough that launch latency
       dominates, so it also runs as one captured CUDA graph.
-cfg4  batched NTT at N = 2^16 over 32 limbs of 31-bit primes (the largest
-      q < 2^31 with q = 1 (mod 2N)), batch 64, int32 residues: [64, N, 1, 32],
-      512 MiB per tensor.
+Int32Ntt        batched NTT at N = 2^16 over 32 limbs of 31-bit primes (the
+      largest q < 2^31 with q = 1 (mod 2N)), batch 64, int32 residues:
+      [64, N, 1, 32], 512 MiB per tensor.
+RaggedBatch     256 ciphertexts of mixed ring degree and limb count, each
+      through the round-trip chain.
 """
 from __future__ import annotations
 
@@ -17,7 +19,7 @@ from . import capi
 from . import params as P
 
 
-class Cfg1:
+class RoundTripChain:
     N, L, BATCH, BOUND = 4096, 4, 8, 1 << 30
 
     def __init__(self, seeds=(101, 102)):
@@ -45,7 +47,7 @@ class Cfg1:
         return 3 * self.BATCH * self.L   # two NTTs and one INTT of 32 limbs each
 
 
-class Cfg4:
+class Int32Ntt:
     N, L, BATCH, BOUND = 1 << 16, 32, 64, 1 << 31
 
     def __init__(self, batch: int | None = None, seed: int = 404):
@@ -77,11 +79,11 @@ class Cfg4:
         return 2 * self.batch * self.N * self.L * 4
 
 
-class Cfg3:
+class RaggedBatch:
     """Ragged batch: `count` ciphertexts [2, N_i, 1, L_i] int64 with N_i drawn
     from 2^logns and L_i uniform in 2..32, under the largest 30-bit primes
     q = 1 (mod 2 N_i) (limb t of every ciphertext of ring degree N uses the
-    t-th such prime).  Every ciphertext runs the cfg1 chain: ntt(A_i),
+    t-th such prime).  Every ciphertext runs the round-trip chain: ntt(A_i),
     ntt(B_i), intt(ntt(A_i)), modmul of the two NTTs, axis_modsum over the
     polynomial axis.  The batch runs as a plain loop of C-ABI calls or as one
     CUDA graph whose branches take the ciphertexts in parallel."""

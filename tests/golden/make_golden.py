@@ -159,7 +159,7 @@ xx = P.residues(24, (2, 16, 1, 2), qs)
 put("ntt_perm", a=xx, p=p, perm=rp, dup=dup, tw=tw, itw=itw, minv=minv, ntt=ref_ntt(xx, p, rp, tw),
     intt=ref_intt(xx, p, rp, itw, minv), ntt_dup=ref_ntt(xx, p, dup, tw), intt_dup=ref_intt(xx, p, dup, itw, minv))
 
-# ---- 3. cfg2-shaped ops at N = 256, 50-bit primes (reference INTT overflows here:
+# ---- 3. keyswitch-shaped ops at N = 256, 50-bit primes (reference INTT overflows here:
 #         its output pins the oracle's literal mode)
 N, L, D, BITS = 256, 4, 3, 17
 qs = P.ntt_primes(2**50, N, L)
@@ -175,7 +175,7 @@ prod = ref_modop("modmul", "ttt", dn, key, qs_t, dn.shape)
 moved = np.moveaxis(prod.reshape(2, N, 1, L, D), 4, 3)  # [2, N, 1, D, L] strided view
 acc = ref_axis_modsum(moved, p, 3)
 gal = P.galois_perm(N, 5).reshape(1, N)
-put("cfg2_small", ct=ct, coef=coef, p=p, perm=perm, tw=tw, itw=itw, minv=minv, key=key,
+put("keyswitch_n256", ct=ct, coef=coef, p=p, perm=perm, tw=tw, itw=itw, minv=minv, key=key,
     ntt_ct=ref_ntt(ct, p, perm, tw), intt_ct_literal=ref_intt(ct, p, perm, itw, minv),
     digits=digits, dn=dn, prod=prod, acc=acc, gal=gal, rot=ref_permute(acc, gal, 2, 1))
 
@@ -235,7 +235,7 @@ RT = ref_intt(NA, p, perm, itw, minv)
 assert np.array_equal(RT, A)
 PR = ref_modop("modmul", "ttt", NA, NB, p, NA.shape)
 AS = ref_axis_modsum(PR, p, 0)
-hashes["cfg1"] = {"N": N, "L": L, "bound": 2**30, "seeds": [101, 102], "shape": [8, N, 1, L],
+hashes["roundtrip_n4096"] = {"N": N, "L": L, "bound": 2**30, "seeds": [101, 102], "shape": [8, N, 1, L],
                   "ntt_a": sha(NA), "ntt_b": sha(NB), "intt_ntt_a": sha(RT), "modmul": sha(PR), "axis_modsum": sha(AS),
                   "ntt_a_head": NA.reshape(-1)[:16].tolist(), "axis_modsum_head": AS.reshape(-1)[:16].tolist()}
 

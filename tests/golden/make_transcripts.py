@@ -69,8 +69,8 @@ def keyswitch(n=256, L=4, D=3, bits=17, bound=50):
     return b.transcript()
 
 
-def cfg1_ops(n=256, L=4, batch=2, bound=30):
-    """The cfg1 chain (ntt, intt, modmul, axis_modsum over the batch) and the
+def roundtrip_ops(n=256, L=4, batch=2, bound=30):
+    """The round-trip chain (ntt, intt, modmul, axis_modsum over the batch) and the
     remaining elementwise and view ops of the dispatcher."""
     qs = P.ntt_primes(1 << bound, n, L)
     p, perm, tw, itw, minv = P.ntt_tables(qs, n)
@@ -87,7 +87,7 @@ def cfg1_ops(n=256, L=4, batch=2, bound=30):
     sl = np.ascontiguousarray(NA[1, 16:48:2, 0, :])          # get_slice(a, 1, slice(16, 48, 2), 0, ...)
 
     b = TranscriptBuilder()
-    b.segment("cfg1")
+    b.segment("roundtrip")
     d = {k: b.host_to_device(T(v)) for k, v in {"A": A, "B": B, "p": p, "perm": perm, "tw": tw, "itw": itw,
                                                "minv": minv}.items()}
     shape = (batch, n, 1, L)
@@ -153,7 +153,7 @@ def matvec(n=256, d=4, L=3, bound=40):
 def main():
     ob.build()
     os.makedirs(OUT, exist_ok=True)
-    for name, fn in (("keyswitch_n256.json", keyswitch), ("cfg1_ops_n256.json", cfg1_ops),
+    for name, fn in (("keyswitch_n256.json", keyswitch), ("roundtrip_ops_n256.json", roundtrip_ops),
                      ("matvec_n256.json", matvec)):
         path = os.path.join(OUT, name)
         save_transcript_to_json(fn(), path)

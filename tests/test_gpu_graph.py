@@ -1,4 +1,4 @@
-"""CUDA graphs of HEAL calls (heal_graph_*): a captured cfg1 step replays
+"""CUDA graphs of HEAL calls (heal_graph_*): a captured round-trip step replays
 bit-exact against the reference's hashes, a capture that would have to
 build a table fails cleanly, and the backend keeps working afterwards."""
 import hashlib
@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from heal_gb300 import capi
-from heal_gb300.configs import Cfg1
+from heal_gb300.configs import RoundTripChain
 from heal_gb300 import params as P
 from _gpu import ready
 
@@ -23,9 +23,9 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def test_captured_cfg1_step_matches_reference(golden_hash):
-    h = golden_hash["cfg1"]
-    c = Cfg1()
+def test_captured_roundtrip_step_matches_reference(golden_hash):
+    h = golden_hash["roundtrip_n4096"]
+    c = RoundTripChain()
     c.run()                      # builds every table the step needs
     for name in ("NA", "NB", "RA", "PR", "AS"):
         getattr(c, name).numpy()

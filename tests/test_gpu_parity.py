@@ -59,8 +59,8 @@ def test_ntt_general_and_duplicate_perm(golden):
     assert np.array_equal(intt(g["a"], g["p"], g["dup"], g["itw"], g["minv"]), g["intt_dup"])
 
 
-def test_cfg2_shaped_chain_golden(golden):
-    g = golden("cfg2_small")
+def test_keyswitch_n256_chain_golden(golden):
+    g = golden("keyswitch_n256")
     p, perm, tw = g["p"], g["perm"], g["tw"]
     assert np.array_equal(ntt(g["ct"], p, perm, tw), g["ntt_ct"])
     x = intt(g["ct"], p, perm, g["itw"], g["minv"])
@@ -125,10 +125,10 @@ def test_permute_golden(golden, tag):
     assert np.array_equal(run("heal_permute", a, g["perms_b"], 0, 3, out_shape=a.shape, dtype=a.dtype), g["r03"])
 
 
-def test_cfg1_full_size_hashes(golden_hash):
+def test_roundtrip_full_size_hashes(golden_hash):
     # [8, 4096, 1, 4] int64 with the four largest 30-bit NTT primes, checked
     # against the reference's own outputs by SHA-256
-    h = golden_hash["cfg1"]
+    h = golden_hash["roundtrip_n4096"]
     qs = P.ntt_primes(h["bound"], h["N"], h["L"])
     p, perm, tw, itw, minv = P.ntt_tables(qs, h["N"])
     A = P.residues(h["seeds"][0], h["shape"], qs)
@@ -324,7 +324,7 @@ def test_g_decomposition_vs_oracle(dt, bits, power):
     capi.synchronize()
 
 
-def test_cfg4_int32_31bit_columns_vs_oracle():
+def test_int32_31bit_columns_vs_oracle():
     # int32 residues under 31-bit primes: the reference's int32 NTT overflows
     # u + q - v here, so the oracle runs in its exact mode (double width)
     m, k = 65536, 4

@@ -11,7 +11,7 @@ import pytest
 
 from heal_gb300 import capi
 from heal_gb300 import params as P
-from heal_gb300.configs import Cfg3
+from heal_gb300.configs import RaggedBatch
 from oracle import oracle as O
 from _gpu import ready, up
 
@@ -44,7 +44,7 @@ def check_against_oracle(c, i):
 
 @pytest.fixture(scope="module")
 def ragged():
-    return Cfg3(count=12, logns=(6, 9, 12, 13, 14), seed=77)
+    return RaggedBatch(count=12, logns=(6, 9, 12, 13, 14), seed=77)
 
 
 def test_ragged_loop_vs_oracle(ragged):

@@ -60,8 +60,8 @@ def test_ntt_general_and_duplicate_perm(golden):
     assert np.array_equal(O.intt(g["a"], g["p"], g["dup"], g["itw"], g["minv"]), g["intt_dup"])
 
 
-def test_cfg2_shaped_chain(golden):
-    g = golden("cfg2_small")
+def test_keyswitch_n256_chain(golden):
+    g = golden("keyswitch_n256")
     p, perm, tw, itw, minv = g["p"], g["perm"], g["tw"], g["itw"], g["minv"]
     assert np.array_equal(O.ntt(g["ct"], p, perm, tw), g["ntt_ct"])
     # the reference's single-width m_inv scaling overflows at 50-bit q: the
@@ -125,8 +125,8 @@ def test_permute_vs_reference(golden, tag):
     assert np.array_equal(O.permute(g["a"], g["perms_b"], 0, 3), g["r03"])
 
 
-def test_cfg1_full_size_hashes(golden_hash):
-    h = golden_hash["cfg1"]
+def test_roundtrip_full_size_hashes(golden_hash):
+    h = golden_hash["roundtrip_n4096"]
     qs = P.ntt_primes(h["bound"], h["N"], h["L"])
     p, perm, tw, itw, minv = P.ntt_tables(qs, h["N"])
     A = P.residues(h["seeds"][0], h["shape"], qs)

@@ -47,7 +47,7 @@ def flat(t):
 
 
 def test_golden_transcripts_exist():
-    assert [os.path.basename(p) for p in GOLD] == ["cfg1_ops_n256.json", "keyswitch_n256.json", "matvec_n256.json"]
+    assert [os.path.basename(p) for p in GOLD] == ["keyswitch_n256.json", "matvec_n256.json", "roundtrip_ops_n256.json"]
 
 
 @pytest.mark.parametrize("path", GOLD, ids=os.path.basename)
@@ -129,7 +129,7 @@ def test_generator_reproduces_the_committed_transcripts(tmp_path):
     code = (f"import runpy, sys; sys.argv=['x']; m = runpy.run_path({gen!r}); "
             f"import heal_gb300.runtime as R; import os; "
             f"[R.save_transcript_to_json(fn(), os.path.join({str(tmp_path)!r}, n)) for n, fn in "
-            f"(('keyswitch_n256.json', m['keyswitch']), ('cfg1_ops_n256.json', m['cfg1_ops']), "
+            f"(('keyswitch_n256.json', m['keyswitch']), ('roundtrip_ops_n256.json', m['roundtrip_ops']), "
             f"('matvec_n256.json', m['matvec']))]")
     subprocess.run([sys.executable, "-c", code], check=True, env=env, cwd=os.path.dirname(HERE))
     for path in GOLD:
