@@ -196,7 +196,9 @@ int heal_mod_ct(int64_t a, const heal_tensor *b, const heal_tensor *result);
  * device looks up that array's device address; make it before any stream
  * capture.  All calls share the array and each overwrites it, so calls that
  * overlap on the GPU (on different streams) race.  A result that overlaps
- * an input in another layout is rejected (it would need a temporary copy). */
+ * an input in another layout is rejected (it would need a temporary copy).
+ * A modulus of 0 gives 0, as in heal_modmul_ttt, but without that call's
+ * warning at the next synchronisation. */
 int heal_modmul_ttt_noalloc(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p,
                             const heal_tensor *result, void *stream);
 
