@@ -215,3 +215,22 @@ def test_permute_errors():
             O.permute(a, perms, ew, pa)
     with pytest.raises(IndexError):
         O.permute(a, np.array([[0, 1, 3], [1, 2, 0]], np.int32), 0, 1)
+
+
+def test_oracle_matches_reference_on_seeded_random_cases():
+    """oracle/crosscheck_ref.py: the oracle's literal mode against HEAL's own
+    example_impl (compiled from its sources into oracle/_ref/) on seeded
+    random shapes, tables and signed inputs of every op. The reference's
+    pybind module runs in its own process: it registers DeviceTensor types
+    under the same names as this backend's module."""
+    import glob
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if not glob.glob(os.path.join(root, "oracle", "_ref", "lattica_hw*.so")):
+        pytest.skip("the reference's sample implementation is not built here (oracle/build_ref.sh)")
+    p = subprocess.run([sys.executable, os.path.join(root, "oracle", "crosscheck_ref.py"), "24"],
+                       capture_output=True, text=True, cwd=root)
+    assert p.returncode == 0, p.stdout[-2000:] + p.stderr[-2000:]
+    assert "bit-exact against the reference" in p.stdout
