@@ -234,3 +234,23 @@ def test_oracle_matches_reference_on_seeded_random_cases():
                        capture_output=True, text=True, cwd=root)
     assert p.returncode == 0, p.stdout[-2000:] + p.stderr[-2000:]
     assert "bit-exact against the reference" in p.stdout
+
+
+@pytest.mark.parametrize("dt,bits,m", [(np.int64, 50, 64), (np.int64, 50, 256), (np.int64, 62, 32),
+                                       (np.int32, 31, 64), (np.int32, 31, 256)])
+def test_exact_mode_is_the_negacyclic_transform(dt, bits, m):
+    """The exact mode (the GPU's contract) checked without the reference, in
+    Python integers: where the reference overflows (50-bit INTT, 31-bit int32
+    NTT and INTT) the forward transform is the natural-order negacyclic DFT
+    out[i] = sum_j a[j] psi^((2i+1) j) mod q, and intt(ntt(a)) = a."""
+    k = 2
+    qs = P.ntt_primes(1 << bits, m, k)
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m, dtype=dt)
+    a = P.residues(31 + m, (1, m, 1, k), qs, dt)
+    fwd = O.ntt(a, p, perm, tw, exact=True)
+    for t, q in enumerate(qs):
+        psi = P.psi(q, m)
+        x = [int(v) for v in a[0, :, 0, t]]
+        want = [sum(x[j] * pow(psi, (2 * i + 1) * j, q) for j in range(m)) % q for i in range(m)]
+        assert [int(v) for v in fwd[0, :, 0, t]] == want, (q, t)
+    assert np.array_equal(O.intt(fwd, p, perm, itw, minv, exact=True), a)
