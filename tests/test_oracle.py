@@ -254,3 +254,26 @@ def test_exact_mode_is_the_negacyclic_transform(dt, bits, m):
         want = [sum(x[j] * pow(psi, (2 * i + 1) * j, q) for j in range(m)) % q for i in range(m)]
         assert [int(v) for v in fwd[0, :, 0, t]] == want, (q, t)
     assert np.array_equal(O.intt(fwd, p, perm, itw, minv, exact=True), a)
+
+
+@pytest.mark.parametrize("dt,bits", [(np.int32, 31), (np.int64, 62)])
+def test_exact_axis_modsum_in_python_integers(dt, bits):
+    """axis_modsum's exact mode: the reference's running truncated sum
+    sum = (sum + a_r) % q, taken in Python integers (no wraparound), for
+    moduli whose 2q exceeds the element type (31-bit int32, 62-bit int64)."""
+    k = 3
+    qs = P.ntt_primes(1 << bits, 8, k)
+    a = P.residues(7, (5, 4, k), qs, dt)
+    a[1] -= np.asarray(qs, dt)      # some negative terms: the truncated % keeps their sign
+    got = O.axis_modsum(a, np.asarray(qs, dt), 0, exact=True)
+
+    def trunc_mod(x, q):
+        r = abs(x) % q
+        return r if x >= 0 else -r
+
+    for i in range(4):
+        for t, q in enumerate(qs):
+            s = 0
+            for r in range(5):
+                s = trunc_mod(s + int(a[r, i, t]), q)
+            assert int(got[i, t]) == s, (i, t)
