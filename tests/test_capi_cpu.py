@@ -123,3 +123,26 @@ def test_ntt_plan_table_host_side():
     finally:
         capi.check(L.heal_ntt_clear_plans())
     assert capi.ntt_plan(np.int64, False, 1 << 16, 24) == (4, 8)
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/heal_gb300.h compiles as C11 on its own (the header a cgo,
+    JNI or N-API binding includes), with every declared entry point callable
+    from C: a C program that takes the address of each links against the
+    library."""
+    import os
+    import subprocess
+    names = capi.declared_symbols()
+    src = tmp_path / "use_header.c"
+    table = "".join(f"  (void (*)(void))&{n},\n" for n in names)
+    src.write_text('#include "heal_gb300.h"\n#include <stdio.h>\n'
+                   f"static void (*const entry[])(void) = {{\n{table}}};\n"
+                   'int main(void) {\n  printf("%zu\\n", sizeof entry / sizeof entry[0]);\n'
+                   "  return entry[0] == 0;\n}\n")
+    inc = os.path.dirname(capi.HEADER)
+    lib_dir = os.path.dirname(capi.LIB_PATH)
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", inc, str(src),
+                    "-o", str(tmp_path / "use_header"), "-L", lib_dir, "-lheal_gb300",
+                    f"-Wl,-rpath,{lib_dir}"], check=True)
+    run = subprocess.run([str(tmp_path / "use_header")], capture_output=True, text=True, check=True)
+    assert int(run.stdout) == len(names)
