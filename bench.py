@@ -50,6 +50,8 @@ CONFIG = {"workload": "keyswitch chain: ct[2][24][65536] int64, 50-bit NTT prime
           "parallelism": "replicas per GPU (limb/ciphertext sharding needs no collective)",
           "streams": "two chains in flight on two CUDA streams (value_one_stream: one stream)"}
 RING = 8
+# the workloads reported under "configs" beside the headline (--configs)
+WORKLOADS = ("roundtrip", "ragged", "int32_ntt", "serving")
 
 
 def dist_info():
@@ -886,7 +888,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default NTT plans instead of autotuned ones")
-    ap.add_argument("--configs", default="roundtrip,ragged,int32_ntt,serving",
+    ap.add_argument("--configs", default=",".join(WORKLOADS),
                     help="comma-separated configurations reported beside the headline")
     ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request", "tail"])
     ap.add_argument("--d", type=int, default=64, help="--mode request: matrix dimension")
@@ -896,6 +898,9 @@ def main():
     ap.add_argument("--inflight", type=int, default=2, help="chains in flight on their own streams")
     ap.add_argument("--probe", default="digits", choices=["digits", "int32", "ct-intt"])
     args = ap.parse_args()
+    unknown = set(args.configs.split(",")) - set(WORKLOADS) - {""}
+    if unknown:
+        ap.error(f"--configs: unknown workload(s) {', '.join(sorted(unknown))}; known: {', '.join(WORKLOADS)}")
     if args.warmup < 3:
         args.warmup = 3
     if args.mode == "ntt":

@@ -60,3 +60,10 @@ def test_reference_arm_under_torchrun_prints_once():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_unknown_workload_names_are_an_argument_error():
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--configs",
+                        "roundtrip,cfg1"], capture_output=True, text=True, cwd=ROOT)
+    assert p.returncode == 2
+    assert "unknown workload(s) cfg1" in p.stderr
