@@ -15,6 +15,10 @@ its overflows. Cases:
   axis_modsum   every legal axis of 2- to 4-axis tensors, signed operands
   g_decomposition  random power and base, non-negative and negative values
   permute       random axes and in-range permutation tables
+  views         random sequences of reshape / expand / squeeze / unsqueeze,
+                the reference's DeviceTensor against this backend's
+                descriptor edits (heal_tensor_*): dims and strides after
+                every step, or the same exception status
 
     python oracle/crosscheck_ref.py [SEEDS]
 
@@ -99,6 +103,95 @@ class Ref:
         out = self.alloc(a.shape, a.dtype)
         self.f("permute", a.dtype)(self.up(a), self.up(perms), out, ew, pa)
         return self.down(a.dtype, out)
+
+
+def ref_metadata(t):
+    """(dims, strides) of a reference DeviceTensor, read from print_metadata
+    (it writes "Shape: [d0 d1 ]  Strides: [s0 s1 ]" to the C++ stdout)."""
+    import ctypes
+    import tempfile
+    libc = ctypes.CDLL(None)
+    sys.stdout.flush()
+    libc.fflush(None)
+    with tempfile.TemporaryFile() as f:
+        saved = os.dup(1)
+        os.dup2(f.fileno(), 1)
+        try:
+            t.print_metadata()
+            libc.fflush(None)
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+        f.seek(0)
+        text = f.read().decode()
+    dims = [int(x) for x in text.split("Shape: [")[1].split("]")[0].split()]
+    strides = [int(x) for x in text.split("Strides: [")[1].split("]")[0].split()]
+    return dims, strides
+
+
+def view_sequences(rng, R, same_views, count):
+    """Random sequences of reshape / expand / squeeze / unsqueeze on a fresh
+    tensor, applied to the reference's DeviceTensor and to this backend's
+    descriptor edits (heal_tensor_*: metadata only, no device memory)."""
+    import ctypes
+    from heal_gb300 import capi
+    L = capi.lib()
+    status_of = {ValueError: 1, IndexError: 2, RuntimeError: 3}
+    for _ in range(count):
+        shape = [int(x) for x in rng.choice([1, 1, 2, 3, 4], size=int(rng.integers(1, 5)))]
+        ref = R.f("allocate_on_hardware", np.int64)(shape)
+        d = capi.desc(None, np.int64, tuple(shape), capi._rowmajor(tuple(shape)))
+        steps = []
+        for _ in range(4):
+            nd = d.ndim
+            kind = ("expand", "squeeze", "unsqueeze", "reshape")[int(rng.integers(0, 4))]
+            if kind == "expand":
+                axis, rep = int(rng.integers(-nd - 1, nd + 1)), int(rng.integers(0, 4))
+                call_ref = lambda: R.f("expand", np.int64)(ref, axis, rep)  # noqa: E731
+                call_ours = lambda: L.heal_tensor_expand(ctypes.byref(d), axis, rep)  # noqa: E731
+                steps.append(f"expand({axis}, {rep})")
+            elif kind == "squeeze":
+                axis = int(rng.integers(-nd - 1, nd + 1))
+                call_ref = lambda: R.f("squeeze", np.int64)(ref, axis)  # noqa: E731
+                call_ours = lambda: L.heal_tensor_squeeze(ctypes.byref(d), axis)  # noqa: E731
+                steps.append(f"squeeze({axis})")
+            elif kind == "unsqueeze":
+                axis = int(rng.integers(-nd - 2, nd + 2))
+                call_ref = lambda: R.f("unsqueeze", np.int64)(ref, axis)  # noqa: E731
+                call_ours = lambda: L.heal_tensor_unsqueeze(ctypes.byref(d), axis)  # noqa: E731
+                steps.append(f"unsqueeze({axis})")
+            else:
+                dims_now = list(d.dims)[:nd]
+                strides_now = list(d.strides)[:nd]
+                # the reference counts elements over the axes whose stride is not 0
+                n = int(np.prod([x for x, st in zip(dims_now, strides_now) if st != 0] or [1]))
+                if rng.random() < 0.3:
+                    n = int(np.prod(dims_now))
+                new = []
+                while n > 1 and len(new) < 4:
+                    f = int(rng.choice([f for f in (2, 3, 4, n) if n % f == 0]))
+                    new.append(f)
+                    n //= f
+                new = new or [1]
+                if rng.random() < 0.3:
+                    new.insert(int(rng.integers(0, len(new) + 1)), 1)
+                arr = (ctypes.c_int64 * len(new))(*new)
+                call_ref = lambda: ref.reshape(new)  # noqa: E731
+                call_ours = lambda: L.heal_tensor_reshape(ctypes.byref(d), len(new), arr)  # noqa: E731
+                steps.append(f"reshape({new})")
+            try:
+                call_ref()
+                ref_status = 0
+            except Exception as e:  # noqa: BLE001  (the pybind-mapped C++ exception)
+                ref_status = status_of.get(type(e), -1)
+            ours = call_ours()
+            ctx = f"start {shape}, ops {steps}"
+            if ref_status or ours:
+                same_views("view_errors", np.array([ours]), np.array([ref_status]), ctx)
+                break
+            got = (list(d.dims)[:d.ndim], list(d.strides)[:d.ndim])
+            same_views("views", np.array(got[0] + [-1] + got[1]),
+                       np.array(ref_metadata(ref)[0] + [-1] + ref_metadata(ref)[1]), ctx)
 
 
 def primes(bits, m, k):
@@ -198,6 +291,7 @@ def run(seeds: int) -> int:
             a = rng.integers(-(1 << 30), 1 << 30, size=shape, dtype=np.int64).astype(dt)
             same("permute", O.permute(a, perms, ew, pa), R.permute(a, perms, ew, pa),
                  f"seed={seed} {np.dtype(dt).name} {shape} ew={ew} pa={pa}")
+    view_sequences(np.random.default_rng(7), R, same, 40 * seeds)
     total = sum(counts.values())
     print(f"crosscheck: {total} cases bit-exact against the reference ({seeds} seeds; " +
           ", ".join(f"{k} {v}" for k, v in sorted(counts.items())) + ")")
