@@ -139,11 +139,16 @@ class LoopStats:
     span: float = 0.0
 
 
-def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max_inflight: int = 64):
+def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max_inflight: int = 64,
+          timeout: float | None = None):
     """Runs the admission loop.  issue(req, offset) enqueues the request's GPU
     work and returns an object with query() -> bool (True once finished) and
     finish() (called once, after query() turned True).  Requests are admitted
-    in arrival order when their footprint fits in the arena."""
+    in arrival order when their footprint fits in the arena.  A request larger
+    than the whole arena raises MemoryError; with `timeout` (seconds), a
+    request still unfinished that long after its admission raises
+    TimeoutError, so a device that stopped answering ends the loop instead
+    of leaving it polling."""
     pending = sorted(requests, key=lambda r: r.arrival)
     queue, inflight, st = [], [], LoopStats()
     nxt, t0 = 0, clock()
@@ -163,6 +168,9 @@ def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max
                 inflight.remove(item)
                 st.latencies.append(req.done - req.arrival)
                 progressed = True
+            elif timeout is not None and now - req.admitted > timeout:
+                raise TimeoutError(f"request {req.rid} unfinished {now - req.admitted:.3f} s after admission "
+                                   f"(limit {timeout} s)")
         while queue and len(inflight) < max_inflight:
             req = queue[0]
             off = arena.alloc(req.footprint())

@@ -98,3 +98,31 @@ def test_request_larger_than_the_arena_fails():
     reqs = [S.Request(0, 0.0, 1 << 15, 16, 256, 0, 0)]
     with pytest.raises(MemoryError):
         S.serve(reqs, S.Arena(1 << 20), lambda r, o: None, clock=FakeClock())
+
+
+def test_unfinished_request_times_out():
+    """A request whose completion never comes (a fake handle that stays
+    unfinished) ends the loop with TimeoutError once the limit has passed;
+    the requests that finished before it were served."""
+    clock = FakeClock()
+    reqs = S.poisson_schedule(5, 1000.0, 3, (256,), (2,), 2, 2, 1, 1)
+
+    class Handle:
+        def __init__(self, req):
+            self.never = req.rid == 2
+
+        def query(self):
+            return not self.never
+
+        def finish(self):
+            pass
+
+    done = []
+    with pytest.raises(TimeoutError, match="request 2 unfinished"):
+        S.serve(reqs, S.Arena(1 << 30), lambda r, o: (done.append(r.rid), Handle(r))[1], clock=clock, timeout=0.01)
+    assert done[:3] == [0, 1, 2]
+    assert all(r.done is not None for r in reqs[:2])
+    # without a limit the same loop is unchanged for requests that finish
+    st = S.serve(S.poisson_schedule(5, 1000.0, 3, (256,), (2,), 2, 2, 1, 1), S.Arena(1 << 30),
+                 lambda r, o: Handle(S.Request(0, 0.0, 256, 2, 2, 0, 0)), clock=FakeClock(), timeout=0.01)
+    assert len(st.latencies) == 5
