@@ -726,6 +726,8 @@ struct NttBatchArgs {
   uint32_t first[kNttBatch + 1];
   NttArgs pass[kNttBatch];
 };
+// a kernel's parameters may take at most 32,764 bytes (CUDA 12.1 and later)
+static_assert(sizeof(NttBatchArgs) <= 32764, "heal_ntt_batch arguments exceed the kernel parameter limit");
 
 template <typename T, int MODE, bool INV, int LOGP>
 __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_batch_kernel(const __grid_constant__ NttBatchArgs b) {
