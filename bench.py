@@ -195,7 +195,9 @@ def profile_traffic():
 
 
 # ------------------------------------------------------------------- CPU
-SAMPLE_LIMBS = 4   # limbs per CPU run: 24 NTT columns, enough to keep every core busy
+# limbs per CPU run of the oracle chain: the INTT gets 2 x 8 = 16 columns and the digit NTT 48, so every
+# core of a 16-core host has work in each step (4 limbs left half of them idle in the INTT); divides 24
+SAMPLE_LIMBS = 8
 
 
 def sample_limbs(run):
