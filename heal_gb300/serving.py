@@ -351,12 +351,15 @@ class MatVecServer:
                     self.alone(Request(rid, 0.0, n, l, d, 0, 0))
         self.torch.cuda.synchronize()
 
-    def run(self, requests, keep=()):
+    def run(self, requests, keep=(), timeout: float | None = 60.0):
+        """Serves `requests`; a request still unfinished `timeout` seconds
+        after its admission (admitted requests take milliseconds) raises
+        TimeoutError."""
         for r in requests:
             r.fused = self.fused
         self.keep = set(keep)
         self.out_host = {}
-        return serve(requests, self.arena, self.issue)
+        return serve(requests, self.arena, self.issue, timeout=timeout)
 
     @staticmethod
     def bytes_moved(req: Request) -> int:
