@@ -98,3 +98,53 @@ def test_headline_shapes_conflict_profile():
         return out
     assert profile(False) == [1, 1, 2]
     assert profile(True) == [2, 1, 2]
+
+
+def _swizzles():
+    """s ^ ((s >> k1) & m1) [^ ((s >> k2) & m2)]: XOR-linear, invertible on
+    every tile (each term moves bits only downward)."""
+    out = []
+    for k1 in range(1, 9):
+        for m1 in (1, 3, 7, 15):
+            out.append(lambda s, k1=k1, m1=m1: s ^ ((s >> k1) & m1))
+    for k1 in range(1, 9):
+        for k2 in range(k1 + 1, 9):
+            for m1 in (3, 7, 15):
+                for m2 in (1, 3, 7, 15):
+                    out.append(lambda s, a=k1, b=k2, x=m1, y=m2: s ^ ((s >> a) & x) ^ ((s >> b) & y))
+    return out
+
+
+def _conflict_free(f, patterns):
+    """No wavefront of any pattern has two distinct words in one bank."""
+    for pts, logc, wb in patterns:
+        C, lanes = 1 << logc, (32 if wb == 4 else 16)
+        words = [(f(p) << logc) + (i & (C - 1)) for i, p in enumerate(pts)]
+        for w0 in range(0, len(words), lanes):
+            by_bank = {}
+            for w in words[w0:w0 + lanes]:
+                by_bank.setdefault((w * wb // 4) % 32, set()).add(w)
+            if any(len(v) > 1 for v in by_bank.values()):
+                return False
+    return True
+
+
+@pytest.mark.parametrize("inv", [False, True])
+def test_each_64bit_exchange_has_a_conflict_free_swizzle(inv):
+    """The next step the 2-way conflicts call for: every exchange of the
+    64-bit modes (the keyswitch chain's transforms), taken on its own, has an
+    XOR swizzle of one or two shifted terms that is conflict-free for both
+    its write pattern (the previous step's layout) and its read pattern, for
+    every tile size and width."""
+    fams = _swizzles()
+    for logp in range(4, 13):
+        for x in range(1, (logp + 2) // 3):
+            pats = []
+            for logc in range(5):
+                threads = ((1 << logp) >> 3) << logc
+                if threads > 512:
+                    continue
+                for st in (x - 1, x):
+                    for e in range(8):
+                        pats.append(([point_of(inv, logp, 3, st, t >> logc, e) for t in range(threads)], logc, 8))
+            assert any(_conflict_free(f, pats) for f in fams), (inv, logp, x)
