@@ -1,26 +1,30 @@
 """Benchmark of the HEAL hot path on one GB300: the keyswitch-shaped chain.
 
-Workload (one step): a ciphertext ct[2][L=24][N=2^16] of int64 residues
-under the 24 largest 50-bit primes q = 1 (mod 2N), through INTT,
-g_decomposition (D = 3 digits of base 2^17), NTT of the 72 digit limbs,
-modmul against a key[3][2][24][2^16], axis_modsum over the digits, and the
-Galois permutation X -> X^5.  Each HEAL call is one C-ABI call.
+Workload: a ciphertext ct[2][L=24][N=2^16] of int64 residues under the 24
+largest 50-bit primes q = 1 (mod 2N), through INTT, g_decomposition (D = 3
+digits of base 2^17), NTT of the 72 digit limbs, modmul against a
+key[3][2][24][2^16], axis_modsum over the digits, and the Galois permutation
+X -> X^5.  Each HEAL call is one C-ABI call.  One step is a batch of
+CHAINS_PER_STEP such chains (ciphertexts rotating through 8 resident inputs),
+so that the driver's 20 timed steps span about half a second.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Printed: one JSON line (rank 0).  `value` is chains/s with inputs resident
 in HBM, timed with CUDA events, consecutive chains alternating between the
-library stream and a second stream (`value_one_stream`: all on one); inputs rotate through
-8 ciphertexts (192 MiB) and 8 outputs, more than the 126 MiB L2, so no step
-reads the previous step's data from L2.  `e2e` is the same through the C ABI
-from pinned host buffers (H2D of ct and D2H of the result of every step
-inside the timed region, on their own streams so that they overlap the
-chains of neighbouring steps; `e2e.serial_value` is the same back to back).
-`roofline` covers the batched NTT of the digits.  `cpu_baseline`
-times the CPU oracle (a restatement of HEAL's example_impl) on this host.
+library stream and a second stream (`value_one_stream`: all on one); inputs
+rotate through 8 ciphertexts (192 MiB) and 8 outputs, more than the 126 MiB
+L2, so no chain reads the previous chain's data from L2.  `e2e` is the same
+through the C ABI from pinned host buffers (H2D of ct and D2H of the result of
+every chain inside the timed region, on their own streams so that they overlap
+the chains of neighbouring steps; `e2e.serial_value` is the same back to
+back).  `roofline` covers the batched NTT of the digits.  `cpu_baseline`
+times the CPU oracle (a restatement of HEAL's example_impl) on this host, on
+SAMPLE_LIMBS of the 24 limbs per run, and compares every limb it computes
+with the GPU chain's output for the same ciphertext (`oracle_equal`).
 
---impl reference times the CPU oracle itself on all host cores, four limbs of
-the chain per step (every limb is independent), scaled to chains/s.
+--impl reference times the CPU oracle itself on all host cores, SAMPLE_LIMBS
+limbs of one chain per step (every limb is independent), scaled to chains/s.
 Under torchrun with N > 1 every rank runs its own chains on its own GPU
 (replicas, no collective on the data path); the time is the max over ranks.
 """
@@ -44,11 +48,13 @@ N, L, D, BITS, BOUND = 1 << 16, 24, 3, 17, 50
 METRIC = "batched NTT limbs/s & keyswitch chains/s on 1 GB300, bit-exact, % HBM roofline"
 CONFIG = {"workload": "keyswitch chain: ct[2][24][65536] int64, 50-bit NTT primes, INTT -> g_decomposition "
                       "(D=3, base 2^17) -> NTT(72 limbs) -> modmul(key[3][2][24][65536]) -> axis_modsum(digits) "
-                      "-> permute(X->X^5)",
+                      "-> permute(X->X^5); one step = 128 such chains",
           "N": N, "limbs": L, "digits": D, "base_bits": BITS, "prime_bits": BOUND,
           "l2": "inputs rotate through 8 ciphertexts (192 MiB) and 8 outputs, larger than L2",
           "parallelism": "replicas per GPU (limb/ciphertext sharding needs no collective)",
-          "streams": "two chains in flight on two CUDA streams (value_one_stream: one stream)"}
+          "streams": "two chains in flight on two CUDA streams (value_one_stream: one stream)",
+          "chains_per_step": 128}
+CHAINS_PER_STEP = CONFIG["chains_per_step"]
 RING = 8
 # the workloads reported under "configs" beside the headline (--configs)
 WORKLOADS = ("roundtrip", "ragged", "int32_ntt", "serving")
@@ -204,20 +210,30 @@ def sample_limbs(run):
     return [(run * SAMPLE_LIMBS + i) % L for i in range(SAMPLE_LIMBS)]
 
 
-def cpu_sample(ch_host, ct, seconds=10.0):
+def cpu_sample(ch_host, ct, seconds=10.0, gpu_out=None):
     """Oracle chain restricted to SAMPLE_LIMBS limbs per run, repeated for
-    ~`seconds`; returns (chains/s, threads, runs)."""
-    from heal_gb300.chain import oracle_chain
+    ~`seconds`; returns (chains/s, threads, runs, check).  With `gpu_out` (the
+    GPU chain's output for `ct`), every limb the oracle computes is compared
+    with the same limb of it; `check` counts the limbs compared and whether
+    all were bit-identical."""
     from oracle import oracle as O
+    from oracle.chain import oracle_chain
     threads = O.set_threads(os.cpu_count() or 1)
-    runs, t0 = 0, time.perf_counter()
+    runs, t0, el = 0, time.perf_counter(), 0.0
+    checked, equal = set(), True
     while True:
-        oracle_chain(ch_host, ct, D, BITS, limb_idx=sample_limbs(runs))
+        li = sample_limbs(runs)
+        t1 = time.perf_counter()
+        got = oracle_chain(ch_host, ct, D, BITS, limb_idx=li)
+        el += time.perf_counter() - t1
+        if gpu_out is not None:
+            equal = equal and bool(np.array_equal(got, gpu_out[..., li]))
+            checked.update(li)
         runs += 1
-        el = time.perf_counter() - t0
-        if el >= seconds:
+        if time.perf_counter() - t0 >= seconds:
             break
-    return runs * SAMPLE_LIMBS / el / L, threads, runs
+    check = None if gpu_out is None else {"oracle_limbs_checked": len(checked), "oracle_equal": equal}
+    return runs * SAMPLE_LIMBS / el / L, threads, runs, check
 
 
 def reference_arm(args):
@@ -225,9 +241,9 @@ def reference_arm(args):
     if rank != 0:
         return 0
     from heal_gb300 import params as P
-    from heal_gb300.chain import oracle_chain
     from oracle import build as ob
     from oracle import oracle as O
+    from oracle.chain import oracle_chain
     ob.build()
     qs = P.ntt_primes(1 << BOUND, N, L)
     p, perm, tw, itw, minv = P.ntt_tables(qs, N)
@@ -243,8 +259,9 @@ def reference_arm(args):
         oracle_chain(host, ct, D, BITS, limb_idx=sample_limbs(s))
     el = time.perf_counter() - t0
     value = args.steps * SAMPLE_LIMBS / el / L
-    sample = (f"{SAMPLE_LIMBS} of the 24 limbs per step (chain output limbs are independent), "
-              f"{args.steps} steps, scaled by {SAMPLE_LIMBS}/24")
+    sample = (f"{SAMPLE_LIMBS} of the 24 limbs of one chain per step (chain output limbs are independent), "
+              f"{args.steps} steps, scaled by {SAMPLE_LIMBS}/24; the oracle restatement of example_impl (the "
+              f"reference's own objects are x86 builds of sources the GPU host does not have)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "chains/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
@@ -345,16 +362,18 @@ def our_arm(args):
         return max_over_ranks(start.elapsed_time(stop), world, "cuda"), capi.launches() - l0
 
     chain_step = lambda s: ch.run(cts[s % RING], outs[s % RING])
-    for w in range(args.warmup):
+    # one timed step is CHAINS_PER_STEP chains; the timed loops below count chains
+    nch = args.steps * CHAINS_PER_STEP
+    for w in range(args.warmup * CHAINS_PER_STEP):
         chain_step2(w)
     with Clocks(local) as clk:
-        ms, launches = timed2(chain_step2, args.steps)
+        ms, launches = timed2(chain_step2, nch)
     clocks = clk.summary()
-    value = whole_job_rate(args.steps, world, ms)
+    value = whole_job_rate(nch, world, ms)
     for w in range(args.warmup):
         chain_step(w)
-    ms_one, _ = timed(chain_step, args.steps)
-    value_one = whole_job_rate(args.steps, world, ms_one)
+    ms_one, _ = timed(chain_step, nch)
+    value_one = whole_job_rate(nch, world, ms_one)
 
     # ---- the same chain fused into 3 calls: intt, heal_g_decomposition_ntt,
     # heal_modmul_axis_sum_permute
@@ -365,18 +384,19 @@ def our_arm(args):
     fused_step = lambda s: ch.run_fused(cts[s % RING], outs[s % RING])
     for w in range(args.warmup):
         fused_step2(w)
-    ms_f2, launches_f = timed2(fused_step2, args.steps)
+    ms_f2, launches_f = timed2(fused_step2, nch)
     for w in range(args.warmup):
         fused_step(w)
-    ms_f1, _ = timed(fused_step, args.steps)
+    ms_f1, _ = timed(fused_step, nch)
     ch.run_fused(cts[0], outs[0])
     assert np.array_equal(outs[0].numpy(), want0), "fused chain differs from the per-call chain"
     tail = lambda s: capi.call("heal_modmul_axis_sum_permute", ch.prod_moved, ch.key_moved, ch.dev["p"], 3,
                                ch.dev["gal"], 2, 1, outs[s % RING])
     for w in range(3):
         tail(w)
-    tail_ms, _ = timed(tail, args.steps)
-    value_f = whole_job_rate(args.steps, world, ms_f2)
+    reps = max(200, args.steps)                      # calls per kernel-level timing
+    tail_ms, _ = timed(tail, reps)
+    value_f = whole_job_rate(nch, world, ms_f2)
     # the fused chain on 8 ciphertexts per call (one [16, N, 1, L] tensor, the key broadcast)
     KB = 8
     kb = ch.batched(KB)
@@ -387,14 +407,14 @@ def our_arm(args):
     assert np.array_equal(kouts[0].numpy()[:2], want0), "batched fused chain differs from the per-call chain"
     for w in range(args.warmup):
         kb.run(kcts[w % 2], kouts[w % 2])
-    ksteps = max(5, args.steps // KB)
+    ksteps = max(5, nch // KB)
     ms_kb, _ = timed(lambda s: kb.run(kcts[s % 2], kouts[s % 2]), ksteps)
     batched_rate = whole_job_rate(ksteps * KB, world, ms_kb)
-    fused_chain = {"value": value_f, "unit": "chains/s", "value_one_stream": whole_job_rate(args.steps, world, ms_f1),
+    fused_chain = {"value": value_f, "unit": "chains/s", "value_one_stream": whole_job_rate(nch, world, ms_f1),
                    "batched_8_per_call": batched_rate,
-                   "vs_per_call": value_f / value, "calls_per_step": 3, "launches_per_step": launches_f / args.steps,
-                   "tail_ms_per_call": tail_ms / args.steps,
-                   "tail_achieved_GBps": (2 * 2 * N * L * D + 2 * N * L) * 8 / (tail_ms / args.steps / 1e3) / 1e9,
+                   "vs_per_call": value_f / value, "calls_per_chain": 3, "launches_per_chain": launches_f / nch,
+                   "tail_ms_per_call": tail_ms / reps,
+                   "tail_achieved_GBps": (2 * 2 * N * L * D + 2 * N * L) * 8 / (tail_ms / reps / 1e3) / 1e9,
                    "hbm_frac": ch.bytes_per_chain_fused() * value_f / world / 1e9 / peaks()[0],
                    "workload": "the same chain in 3 calls: intt; g_decomposition -> ntt as one "
                                "heal_g_decomposition_ntt; modmul(key) -> axis_modsum(digits) -> permute as one "
@@ -405,8 +425,8 @@ def our_arm(args):
                                    None, None, ch.dn)
     for w in range(3):
         ntt_step(w)
-    ntt_ms, ntt_launches = timed(ntt_step, args.steps)
-    ntt_call_ms = ntt_ms / args.steps
+    ntt_ms, ntt_launches = timed(ntt_step, reps)
+    ntt_call_ms = ntt_ms / reps
     limbs_per_call = 2 * L * D
     ntt_bytes = 2 * limbs_per_call * N * 8           # read + write of every limb once
     hbm, peak_kind = peaks()
@@ -434,15 +454,16 @@ def our_arm(args):
              lambda s: capi.call("heal_modmul_ttt", ch.dn, d["key"], d["p_t"], ch.dn),
              lambda s: capi.call("heal_axis_modsum", ch.prod_moved, d["p"], ch.acc, 3),
              lambda s: capi.call("heal_permute", ch.acc, d["gal"], outs[s % RING], 2, 1)]
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(calls) + 1)] for _ in range(args.steps)]
+    nsplit = 50
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(calls) + 1)] for _ in range(nsplit)]
     barrier()
-    for s in range(args.steps):
+    for s in range(nsplit):
         evs[s][0].record(stream)
         for ci, fn in enumerate(calls):
             fn(s)
             evs[s][ci + 1].record(stream)
     torch.cuda.synchronize()
-    split_ms = {n: statistics.median(evs[s][ci].elapsed_time(evs[s][ci + 1]) for s in range(args.steps))
+    split_ms = {n: statistics.median(evs[s][ci].elapsed_time(evs[s][ci + 1]) for s in range(nsplit))
                 for ci, n in enumerate(names)}
 
     # ---- end to end through the C ABI from pinned host memory.  Every step
@@ -499,8 +520,8 @@ def our_arm(args):
 
     for w in range(args.warmup):
         e2e_step(w)
-    e2e_ms = e2e_timed(args.steps)
-    e2e = whole_job_rate(args.steps, world, e2e_ms)
+    e2e_ms = e2e_timed(nch)
+    e2e = whole_job_rate(nch, world, e2e_ms)
     torch.cuda.synchronize()
     want = outs[0].numpy()
     for p_ in pin_out:
@@ -515,8 +536,8 @@ def our_arm(args):
 
     for w in range(args.warmup):
         serial_step(w)
-    serial_ms, _ = timed(serial_step, args.steps)
-    e2e_serial = whole_job_rate(args.steps, world, serial_ms)
+    serial_ms, _ = timed(serial_step, nch)
+    e2e_serial = whole_job_rate(nch, world, serial_ms)
     capi.lib().heal_host_free(pin_in)
     for p_ in pin_out:
         capi.lib().heal_host_free(p_)
@@ -529,18 +550,18 @@ def our_arm(args):
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if world == 1 and not args.skip_cpu:
-        v, threads, runs = cpu_sample(ch.host, cts_host[0], seconds=args.cpu_seconds)
+        v, threads, runs, check = cpu_sample(ch.host, cts_host[0], seconds=args.cpu_seconds, gpu_out=want0)
         cpu = {"value": v, "unit": "chains/s", "cores": threads, "kind": "port",
                "sample": f"CPU oracle chain on {SAMPLE_LIMBS} of the 24 limbs per run ({runs} runs, "
-                         f"~{args.cpu_seconds:.0f} s), scaled by {SAMPLE_LIMBS}/24"}
+                         f"~{args.cpu_seconds:.0f} s), scaled by {SAMPLE_LIMBS}/24; every limb it computes is "
+                         f"compared with the GPU chain's output for the same ciphertext", **check}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "chains/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
-                "config": dict(CONFIG, streams=f"{K} chains in flight on {K} CUDA streams (value_one_stream: one "
-                                               f"stream)"), "value_one_stream": value_one,
-                "ntt_limbs_per_s": limbs_per_call * args.steps * world / (ntt_ms / 1e3),
+                "config": CONFIG, "chains_in_flight": K, "value_one_stream": value_one,
+                "ntt_limbs_per_s": limbs_per_call * reps * world / (ntt_ms / 1e3),
                 "chain_hbm_frac": chain_bytes * value / world / 1e9 / hbm,
                 "roofline": {"bound": "hbm", "kernel": "heal_ntt of the 72 digit limbs ([2, 65536, 1, 72] int64)",
                              "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
@@ -548,7 +569,8 @@ def our_arm(args):
                              "ms_per_call": ntt_call_ms,
                              "traffic": traffic.get("bytes_per_call") if traffic else None},
                 "int_roofline": int_roofline,
-                "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes * CHAINS_PER_STEP,
+                        "d2h_bytes_per_step": nbytes * CHAINS_PER_STEP,
                         "pipeline": "H2D and D2H on their own streams, consecutive chains alternating between two "
                                     "compute streams",
                         "serial_value": e2e_serial},
@@ -578,17 +600,44 @@ def other_configs(args, timed, stream):
     return out
 
 
+def cpu_run(fn, seconds):
+    """Calls fn() until ~`seconds` have passed (at least once); returns
+    (seconds per call, calls, threads).  The oracle uses every host core."""
+    from oracle import oracle as O
+    threads = O.set_threads(os.cpu_count() or 1)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        fn()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            return el / n, n, threads
+
+
+def hbm_roofline(nbytes, ms, kernel, note=None):
+    """The `roofline` object of a workload timed as a whole: algorithmic bytes
+    over its CUDA-event time against the measured HBM copy bandwidth."""
+    hbm, kind = peaks()
+    achieved = nbytes / (ms / 1e3) / 1e9
+    r = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
+         "frac": achieved / hbm, "algorithmic_bytes": nbytes, "traffic": None}
+    if note:
+        r["note"] = note
+    return r
+
+
 def roundtrip_config(args, timed):
     import hashlib
     from heal_gb300 import capi
     from heal_gb300.configs import RoundTripChain
+    from oracle.chain import oracle_roundtrip
     c1 = RoundTripChain()
     c1.run()
     with open(os.path.join(ROOT, "tests", "golden", "golden_hash.json")) as f:
         gh = json.load(f)["roundtrip_n4096"]
     sha = lambda a: hashlib.sha256(np.ascontiguousarray(a.numpy()).tobytes()).hexdigest()
     exact = sha(c1.NA) == gh["ntt_a"] and sha(c1.AS) == gh["axis_modsum"] and sha(c1.RA) == gh["intt_ntt_a"]
-    steps = max(args.steps, 50)
+    steps = max(args.steps, 200)
     for _ in range(3):
         c1.run()
     ms_plain, l_plain = timed(lambda s: c1.run(), steps)
@@ -597,27 +646,56 @@ def roundtrip_config(args, timed):
         graph.launch()
     ms_graph, l_graph = timed(lambda s: graph.launch(), steps)
     exact = exact and sha(c1.AS) == gh["axis_modsum"]
+    t = {k: v.numpy() for k, v in c1.t.items()}
+    want = oracle_roundtrip(c1.host["A"], c1.host["B"], t["p"], t["perm"], t["tw"], t["itw"], t["minv"])
+    oracle_equal = all(np.array_equal(w, g.numpy()) for w, g in zip(want, (c1.NA, c1.NB, c1.RA, c1.PR, c1.AS)))
+    cpu_s, runs, threads = cpu_run(lambda: oracle_roundtrip(c1.host["A"], c1.host["B"], t["p"], t["perm"], t["tw"],
+                                                            t["itw"], t["minv"]), 3.0)
+    step_ms = ms_graph / steps
     return {"workload": "ntt(A), ntt(B), intt(ntt(A)), modmul, axis_modsum over the batch; [8, 4096, 1, 4] "
                         "int64, 30-bit primes", "bit_exact_vs_reference_hashes": exact,
-            "step_us_plain": ms_plain / steps * 1e3, "step_us_graph": ms_graph / steps * 1e3,
+            "oracle_equal": oracle_equal,
+            "step_us_plain": ms_plain / steps * 1e3, "step_us_graph": step_ms * 1e3,
             "transform_limbs_per_s_graph": c1.transform_limbs() * steps / (ms_graph / 1e3),
-            "launches_per_step": l_graph / steps}
+            "launches_per_step": l_graph / steps,
+            "roofline": hbm_roofline(c1.bytes_per_step(), step_ms, "the captured step (5 calls)",
+                                     "the 10.6 MB step is L2-resident; launch latency bounds it"),
+            "cpu_baseline": {"value": c1.transform_limbs() / cpu_s, "unit": "transform limbs/s", "cores": threads,
+                             "kind": "port", "step_us": cpu_s * 1e6,
+                             "sample": f"the whole step on the oracle, {runs} runs"}}
 
 
 def int32_ntt_config(args, timed):
     from heal_gb300.configs import Int32Ntt
+    from oracle import oracle as O
     c4 = Int32Ntt()
     c4.ntt()
     c4.intt()
-    round_trip = bool(np.array_equal(c4.Z.numpy()[:2], c4.host_x[:2]))
-    st4 = max(10, args.steps // 10)
+    # full-shape parity: two of the 64 batch rows (64 limb-polynomials of 2^16 points) against the oracle's
+    # 64-bit transform of the same residues widened to int64 (exact for q < 2^31)
+    t = c4.host_tables
+    wide = lambda a: np.asarray(a, np.int64)
+    x2 = wide(c4.host_x[:2])
+    want = O.ntt(x2, wide(t["p"]), wide(t["perm"]), wide(t["tw"]))
+    got = c4.Y.numpy()[:2]
+    ntt_equal = bool(np.array_equal(got.astype(np.int64), want))
+    inv_want = O.intt(want, wide(t["p"]), wide(t["perm"]), wide(t["itw"]), wide(t["minv"]))
+    intt_equal = bool(np.array_equal(c4.Z.numpy()[:2].astype(np.int64), inv_want))
+    round_trip = bool(np.array_equal(c4.Z.numpy(), c4.host_x))
+    st4 = max(20, args.steps)
     ms4, _ = timed(lambda s: c4.ntt(), st4)
     ms4i, _ = timed(lambda s: c4.intt(), st4)
-    hbm, _ = peaks()
     per = ms4 / st4
+    x1 = wide(c4.host_x[:1])
+    cpu_s, runs, threads = cpu_run(lambda: O.ntt(x1, wide(t["p"]), wide(t["perm"]), wide(t["tw"])), 5.0)
     return {"workload": "ntt on [64, 65536, 1, 32] int32, 31-bit primes, radix-8 Shoup butterflies on the integer "
                         "pipes", "ntt_ms": per, "intt_ms": ms4i / st4, "limbs_per_s": c4.limbs() / (per / 1e3),
-            "hbm_frac": c4.bytes_per_call() / (per / 1e3) / 1e9 / hbm, "round_trip_exact": round_trip,
+            "oracle_equal": {"ntt_rows_0_1": ntt_equal, "intt_rows_0_1": intt_equal},
+            "round_trip_exact": round_trip,
+            "roofline": hbm_roofline(c4.bytes_per_call(), per, "heal_ntt of [64, 65536, 1, 32] int32 (two passes)"),
+            "cpu_baseline": {"value": c4.L / cpu_s, "unit": "limbs/s", "cores": threads, "kind": "port",
+                             "sample": f"the oracle's 64-bit NTT of one batch row (32 limbs) widened to int64, "
+                                       f"{runs} runs"},
             "tensor_core_floor": tensor_floor(c4.limbs(), per)}
 
 
@@ -705,6 +783,21 @@ def ragged_config(args, timed):
     del gb
     round_trip = all(np.array_equal(c3.RA[i].numpy(), c3.A[i].numpy()) for i in range(len(c3.specs)))
     best = min(res[1][0], res[8][0], ms_bgraph / steps)
+    # oracle parity and CPU baseline on every 32nd ciphertext (8 of 256, every ring degree present), the
+    # CPU time scaled to the whole batch by algorithmic bytes
+    from oracle.chain import oracle_roundtrip
+    sample = list(range(0, len(c3.specs), 32))
+    host = {i: (c3.A[i].numpy(), c3.B[i].numpy(), {k: v.numpy() for k, v in c3.views[i].items()}) for i in sample}
+    oracle_equal = True
+    for i in sample:
+        a_, b_, v = host[i]
+        want = oracle_roundtrip(a_, b_, v["p"], v["perm"], v["tw"], v["itw"], v["minv"])
+        oracle_equal = oracle_equal and all(np.array_equal(w, g.numpy()) for w, g in
+                                            zip(want, (c3.NA[i], c3.NB[i], c3.RA[i], c3.PR[i], c3.AS[i])))
+    cpu_s, runs, threads = cpu_run(lambda: [oracle_roundtrip(host[i][0], host[i][1], *(host[i][2][k] for k in
+                                                             ("p", "perm", "tw", "itw", "minv"))) for i in sample],
+                                   5.0)
+    scale = c3.bytes_per_step() / sum(c3.bytes_of(i) for i in sample)
     shapes = sorted(plans)
     return {"workload": "256 ciphertexts [2, N, 1, L] int64, N in 2^12..2^16, L uniform in 2..32, 30-bit primes; "
                         "ntt(A), ntt(B), intt(ntt(A)), modmul, axis_modsum per ciphertext (1280 calls per step)",
@@ -721,6 +814,11 @@ def ragged_config(args, timed):
             "hbm_frac": c3.bytes_per_step() / (best / 1e3) / 1e9 / hbm,
             "launches_per_step": res[8][1], "plain_launches_per_step": l_plain / steps,
             "graph_equals_loop": res[1][2] and res[8][2], "round_trip_exact": round_trip,
+            "oracle_equal": {"ciphertexts_checked": len(sample), "equal": oracle_equal},
+            "roofline": hbm_roofline(c3.bytes_per_step(), best, "the fastest form of the step"),
+            "cpu_baseline": {"value": len(c3.specs) / (cpu_s * scale), "unit": "ciphertexts/s", "cores": threads,
+                             "kind": "port", "sample": f"the oracle chain on {len(sample)} of the 256 ciphertexts "
+                                                       f"({runs} runs), scaled to the batch by algorithmic bytes"},
             "autotuned_shapes": len(shapes), "autotune_s": tune_s, "setup_s": setup_s,
             "plans_sample": {f"{n}x{l}": {"fwd": plans[(n, l)][0], "inv": plans[(n, l)][1]}
                              for n, l in shapes[:: max(1, len(shapes) // 6)]}}
@@ -729,33 +827,68 @@ def ragged_config(args, timed):
 def serving_config(args, count: int = 4000, rate: float = 2000.0):
     """Serving loop: Poisson arrivals of ciphertext x plaintext-matrix products
     admitted by HBM footprint; served with the three HEAL calls (permute
-    rotations, modmul, axis_modsum) and with the fused modmul_axis_sum."""
+    rotations, modmul, axis_modsum) and with the fused modmul_axis_sum.  The
+    fused path is then offered the same schedule at rising rates until it
+    saturates (throughput below 90% of the offered rate), which measures its
+    capacity and where its p99 latency breaks."""
+    from heal_gb300 import serving as S
     out = {"workload": f"{count} Poisson arrivals at {rate:.0f}/s of ct[2][N][L] x (d x d plaintext matrix): "
                        "d in {16, 64, 256}, N in {2^14, 2^15}, L uniform in 8..16, 40-bit primes; sum over d Galois "
                        "rotations of rot_i(ct) * diag_i, H2D of the matrix and D2H of the result per request"}
     for name, fused in (("three_calls", False), ("fused", True)):
-        out[name] = serve_once(count, rate, fused)
+        srv, setup_s = serving_server(fused)
+        out[name] = serve_once(srv, count, rate, setup_s)
+        if fused:
+            sweep = []
+            for r in (4000.0, 8000.0, 16000.0, 32000.0, 64000.0):
+                res = serve_once(srv, count, r, setup_s, detail=False)
+                sweep.append(res)
+                if res["throughput_req_per_s"] < 0.9 * res["offered_req_per_s"]:
+                    break
+            out["fused_rate_sweep"] = sweep
+            out["fused_capacity_req_per_s"] = max(x["throughput_req_per_s"] for x in sweep + [out[name]])
+            out["cpu_baseline"] = serving_cpu(srv)
+            out["roofline"] = dict(hbm_roofline(out[name]["algorithmic_GBps"] * 1e9, 1e3,
+                                                "the fused serving loop at the offered rate"),
+                                   note="achieved = algorithmic bytes of the served requests over the run's span; "
+                                        "the loop is bound by the offered load, not by HBM")
+        del srv
     return out
 
 
-def serve_once(count, rate, fused):
-    import torch
+def serving_server(fused):
     from heal_gb300 import serving as S
     t0 = time.time()
     srv = S.MatVecServer(fused=fused)
     srv.warm()
-    setup_s = time.time() - t0
-    alone_ms = {}
-    for d in srv.ds:                                   # service time of the largest request of each d
-        r = S.Request(-1, 0.0, max(srv.ns), srv.lmax, d, 0, 0)
-        ts = []
-        for _ in range(5):
-            t1 = time.perf_counter()
-            srv.alone(r)
-            ts.append((time.perf_counter() - t1) * 1e3)
-        alone_ms[str(d)] = statistics.median(ts)
-    big = S.Request(-1, 0.0, max(srv.ns), srv.lmax, max(srv.ds), 0, 0)
-    split = srv.split_ms(big)
+    return srv, time.time() - t0
+
+
+def serving_cpu(srv):
+    """The oracle's service rate for the request mix: one request of each d at
+    N = 2^14, L = 8 timed on the oracle (permute, modmul, axis_modsum on every
+    host core), the time per multiply-add fitted over the three and scaled to
+    the mix's mean request (E[d] E[N] E[L], the draws being independent)."""
+    from oracle.chain import oracle_matvec
+    n, l = min(srv.ns), srv.lmin
+    ct = srv.ct[(n, l)][0].numpy()
+    p = np.array(srv.qs[n][:l], np.int64)
+    work, secs, threads = 0, 0.0, 1
+    for d in srv.ds:
+        t, _, threads = cpu_run(lambda: oracle_matvec(ct, srv.perms[(n, d)].numpy(),
+                                                      srv.host_mats[(d, l, 0)][n].numpy(), p), 0.5)
+        work += 2 * d * n * l
+        secs += t
+    mean_work = 2 * np.mean(srv.ds) * np.mean(srv.ns) * (srv.lmin + srv.lmax) / 2
+    return {"value": 1.0 / (secs / work * mean_work), "unit": "req/s", "cores": threads, "kind": "port",
+            "sample": f"one request per d in {list(srv.ds)} at N={n}, L={l} on the oracle; scaled to the mean "
+                      f"request of the mix by multiply-adds, requests served one after another"}
+
+
+def serve_once(srv, count, rate, setup_s, detail=True):
+    import torch
+    from heal_gb300 import serving as S
+    fused = srv.fused
     reqs = S.poisson_schedule(count, rate, 606, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
     sample = [r.rid for r in reqs[:: count // 8]]
     st = srv.run(reqs, keep=sample)
@@ -768,10 +901,22 @@ def serve_once(count, rate, fused):
            "p50_wait_ms": ms(st.waits, 50), "p99_wait_ms": ms(st.waits, 99),
            "throughput_req_per_s": count / st.span, "offered_req_per_s": count / reqs[-1].arrival,
            "algorithmic_GBps": moved / st.span / 1e9, "max_inflight": st.max_inflight, "max_queue": st.max_queue,
-           "arena_GiB": srv.arena_size / 2**30, "peak_arena_GiB": st.peak_bytes / 2**30, "streams": len(srv.streams),
-           "service_ms_alone_largest": alone_ms, "alone_equals_mix": same, "setup_s": setup_s,
-           "split_ms_largest": split, "largest_request_bytes": S.MatVecServer.bytes_moved(big)}
-    del srv
+           "alone_equals_mix": same}
+    if not detail:
+        return res
+    alone_ms = {}
+    for d in srv.ds:                                   # service time of the largest request of each d
+        r = S.Request(-1, 0.0, max(srv.ns), srv.lmax, d, 0, 0)
+        ts = []
+        for _ in range(5):
+            t1 = time.perf_counter()
+            srv.alone(r)
+            ts.append((time.perf_counter() - t1) * 1e3)
+        alone_ms[str(d)] = statistics.median(ts)
+    big = S.Request(-1, 0.0, max(srv.ns), srv.lmax, max(srv.ds), 0, 0)
+    res.update({"arena_GiB": srv.arena_size / 2**30, "peak_arena_GiB": st.peak_bytes / 2**30,
+                "streams": len(srv.streams), "service_ms_alone_largest": alone_ms, "setup_s": setup_s,
+                "split_ms_largest": srv.split_ms(big), "largest_request_bytes": S.MatVecServer.bytes_moved(big)})
     return res
 
 
@@ -883,7 +1028,7 @@ def ntt_probe(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=20, help="timed steps (a chain step is CHAINS_PER_STEP chains)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

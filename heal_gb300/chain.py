@@ -157,28 +157,3 @@ class KeyswitchBatch:
         o = out.reshape((self.count, 2, ch.n, 1, ch.L))
         capi.call("heal_modmul_axis_sum_permute", self.dn_moved, self.key_moved, d["p"], 4, self.gal2, 1, 2, o)
 
-
-def oracle_chain(ch_host: dict, ct: np.ndarray, digits: int, base_bits: int, limb_idx=None):
-    """The same chain on the CPU oracle (tests / bench baseline only).  With
-    `limb_idx`, only those limbs are computed: every output limb depends only
-    on its own input limb and key columns."""
-    from oracle import oracle as O
-    h = ch_host
-    p, perm, tw, itw, minv = h["p"], h["perm"], h["tw"], h["itw"], h["minv"]
-    key = h["key"]
-    L = len(p)
-    if limb_idx is not None:
-        li = np.asarray(limb_idx)
-        cols = (li[:, None] * digits + np.arange(digits)[None, :]).reshape(-1)
-        p, tw, itw, minv = p[li], tw[li], itw[li], minv[li]
-        key = key[..., cols]
-        ct = ct[..., li]
-        L = len(li)
-    x = O.intt(np.ascontiguousarray(ct), p, perm, itw, minv)
-    dig, _ = O.g_decomposition(x, digits, base_bits)
-    n = ct.shape[1]
-    p_t = np.repeat(p, digits)
-    dn = O.ntt(dig.reshape(2, n, 1, L * digits), p_t, perm, np.repeat(tw, digits, axis=0))
-    prod = O.modmul(dn, np.ascontiguousarray(key), p_t)
-    acc = O.axis_modsum(np.moveaxis(prod.reshape(2, n, 1, L, digits), 4, 3), p, 3)
-    return O.permute(acc, h["gal"], 2, 1)

@@ -46,6 +46,13 @@ class RoundTripChain:
     def transform_limbs(self) -> int:
         return 3 * self.BATCH * self.L   # two NTTs and one INTT of 32 limbs each
 
+    def bytes_per_step(self) -> int:
+        """Algorithmic bytes of one step: three transforms (read + write of a
+        [8, 4096, 1, 4] int64 tensor each), modmul (two reads, one write),
+        axis_modsum (one read, one write of a [4096, 1, 4] tensor)."""
+        t = self.BATCH * self.N * self.L * 8
+        return 3 * 2 * t + 3 * t + t + t // self.BATCH
+
 
 class Int32Ntt:
     N, L, BATCH, BOUND = 1 << 16, 32, 64, 1 << 31
@@ -230,8 +237,13 @@ class RaggedBatch:
     def transform_limbs(self) -> int:
         return sum(3 * 2 * l for _, l in self.specs)
 
-    def bytes_per_step(self) -> int:
-        """Algorithmic bytes of one pass over the batch: three transforms (read
-        + write), modmul (two reads, one write), axis_modsum (read of both
+    def bytes_of(self, i: int) -> int:
+        """Algorithmic bytes of ciphertext i's chain: three transforms (read +
+        write), modmul (two reads, one write), axis_modsum (read of both
         polynomials, write of one)."""
-        return sum(2 * n * l * 8 * (2 + 2 + 2 + 3) + (2 * n * l + n * l) * 8 for n, l in self.specs)
+        n, l = self.specs[i]
+        return 2 * n * l * 8 * (2 + 2 + 2 + 3) + (2 * n * l + n * l) * 8
+
+    def bytes_per_step(self) -> int:
+        """Algorithmic bytes of one pass over the batch."""
+        return sum(self.bytes_of(i) for i in range(len(self.specs)))

@@ -779,6 +779,12 @@ static int modmul_noalloc(const heal_tensor *a, const heal_tensor *b, const heal
                        "heal_modmul_ttt_noalloc: result overlaps an input in another layout (that needs a copy)");
   const int64_t n = numel(*r);
   if (n == 0) return HEAL_OK;
+  // the launch checks below read the calling thread's last CUDA error: one
+  // left pending by an earlier call (another library, another stream) is
+  // reported as that, not as a failure of this call's launches
+  const cudaError_t pending = cudaGetLastError();
+  if (pending != cudaSuccess)
+    return cuda_fail(pending, "heal_modmul_ttt_noalloc: a CUDA error left pending by an earlier call on this thread");
   NoAllocDevice *dev = nullptr;
   HEAL_CHECK(noalloc_setup(&dev));
   cudaStream_t s = (cudaStream_t)stream_ptr;

@@ -198,7 +198,11 @@ int heal_mod_ct(int64_t a, const heal_tensor *b, const heal_tensor *result);
  * overlap on the GPU (on different streams) race.  A result that overlaps
  * an input in another layout is rejected (it would need a temporary copy).
  * A modulus of 0 gives 0, as in heal_modmul_ttt, but without that call's
- * warning at the next synchronisation. */
+ * warning at the next synchronisation.  The result is written on `stream`;
+ * when another library call then reads it on the library stream (for
+ * instance as moduli or twiddles), order the two streams with an event or a
+ * synchronisation first.  A CUDA error left pending on the calling thread by
+ * an earlier call is returned as HEAL_ERR_RUNTIME before anything runs. */
 int heal_modmul_ttt_noalloc(const heal_tensor *a, const heal_tensor *b, const heal_tensor *p,
                             const heal_tensor *result, void *stream);
 

@@ -1,12 +1,14 @@
 #!/usr/bin/env bash
 # Builds HEAL's own sample implementation (example_impl + py_bindings) from
 # the reference sources where they lie, into oracle/_ref/ (git-ignored).
+# The reference location is the first argument, else HEAL_REFERENCE, else
+# the development container's checkout (oracle/reference.py finds the same).
 # Used only in the development container to pin the oracle and to write the
 # golden fixtures under tests/golden/; the GPU host never has the sources.
 # The reference's CMake forces _GLIBCXX_USE_CXX11_ABI=0 (CMakeLists.txt:11),
 # which does not match the installed torch, so it is compiled directly here.
 set -euo pipefail
-REF=${HEAL_REFERENCE:-/root/reference}
+REF=${1:-${HEAL_REFERENCE:-/root/reference}}
 OUT="$(cd "$(dirname "$0")" && pwd)/_ref"
 [ -d "$REF/example_impl" ] || { echo "reference sources not found at $REF" >&2; exit 1; }
 mkdir -p "$OUT"

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from heal_gb300 import serving as S
-from oracle import oracle as O
+from oracle.chain import oracle_matvec
 from _gpu import ready
 
 pytestmark = pytest.mark.gpu
@@ -19,13 +19,8 @@ def gpu():
 
 def oracle_product(srv, req):
     n, l, d = req.n, req.l, req.d
-    ct = srv.ct[(n, l)][req.ct].numpy()
-    perms = srv.perms[(n, d)].numpy()
-    diag = srv.host_mats[(d, l, req.mat)][n].numpy()
-    p = np.array(srv.qs[n][:l], np.int64)
-    stack = O.permute(np.ascontiguousarray(np.broadcast_to(ct[None], (d, 2, n, l))), perms, 0, 2)
-    prod = O.modmul(stack.reshape(d, 2, n // d, d, l), diag, p)
-    return O.axis_modsum(prod.reshape(d, 2, n, l), p, 0)
+    return oracle_matvec(srv.ct[(n, l)][req.ct].numpy(), srv.perms[(n, d)].numpy(),
+                         srv.host_mats[(d, l, req.mat)][n].numpy(), np.array(srv.qs[n][:l], np.int64))
 
 
 @pytest.mark.parametrize("fused", [False, True])

@@ -18,7 +18,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, os.path.join(ROOT, "tests", "native"))
 import heal_suite  # noqa: E402
 
-HEAL_DIR = os.environ.get("HEAL_REFERENCE", "/root/reference")
+from oracle import reference  # noqa: E402
+
+HEAL_DIR = reference.path() or ""
 
 
 def _symbols(path, undefined):
@@ -32,7 +34,7 @@ def _heal(sym):
         sym.startswith("_ZNK12DeviceTensor")
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(HEAL_DIR, "tests")), reason="HEAL's sources are not present")
+@pytest.mark.skipif(not HEAL_DIR or not os.path.isdir(os.path.join(HEAL_DIR, "tests")), reason="HEAL's sources are not present")
 def test_heal_test_suite_links_against_this_backend(tmp_path):
     exes = heal_suite.build(HEAL_DIR, str(tmp_path))
     assert len(exes) == 10, sorted(exes)

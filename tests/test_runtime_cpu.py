@@ -17,7 +17,9 @@ from heal_gb300.runtime.executor import VerificationError, run_transcript
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = sorted(glob.glob(os.path.join(HERE, "golden", "transcripts", "*.json")))
-REF_RUNTIME = "/root/reference/python_execution"
+from oracle import reference  # noqa: E402
+
+REF_RUNTIME = os.path.join(reference.path(), "python_execution") if reference.path() else ""
 
 
 def flat(t):
