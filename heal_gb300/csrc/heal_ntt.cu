@@ -52,6 +52,30 @@ int launch_ntt_pass_inv32(const NttArgs &a, int64_t nblocks, int mode);
 int launch_ntt_pass_inv64(const NttArgs &a, int64_t nblocks, int mode);
 int launch_ntt_pass_fwd32_gdec(const NttArgs &a, int64_t nblocks, int mode);
 int launch_ntt_pass_fwd64_gdec(const NttArgs &a, int64_t nblocks, int mode);
+int launch_ntt_staged_fwd32(const NttArgs &a, int mode);
+int launch_ntt_staged_inv32(const NttArgs &a, int mode);
+
+// Passes the staged kernel (heal_ntt_staged.cuh) takes: 256-point passes of
+// int32 tensors (the 32-bit word modes, where it measured faster than the
+// register kernel), limbs contiguous in source and destination with every
+// 16-byte row chunk aligned, no permutation or the bit reversal, no gather
+// after the pass, no g_decomposition on load.  HEAL_NTT_STAGED=0 in the
+// environment keeps every pass on the register kernel (for comparisons).
+static bool staged_eligible(const NttArgs &a, bool is32, int mode) {
+  static const bool on = [] {
+    const char *e = getenv("HEAL_NTT_STAGED");
+    return !e || atoi(e) != 0;
+  }();
+  if (!on || a.p != 8 || a.gdec_power || a.store_gather) return false;
+  if ((a.load_map || a.store_scatter) && !a.bitrev) return false;
+  if (!is32 || !(mode == MODE_N32 || mode == MODE_N32_LAZY)) return false;
+  const int64_t esz = 4;
+  if (a.ss[3] != 1 || a.ds[3] != 1 || a.k % (16 / esz)) return false;
+  auto aligned = [&](const void *ptr, const int64_t *st) {
+    return (uintptr_t)ptr % 16 == 0 && (st[0] * esz) % 16 == 0 && (st[1] * esz) % 16 == 0 && (st[2] * esz) % 16 == 0;
+  };
+  return aligned(a.src, a.ss) && aligned(a.dst, a.ds);
+}
 
 // out[i, u, j, t] = src[i, perm[u], j, t] (forward NTT with a non-bijective
 // permutation after the two-pass transform)
@@ -133,6 +157,7 @@ static int launch_any(const NttArgs &a, int64_t nblocks, bool is32, int mode, bo
 }
 
 static int launch_now(const NttArgs &a, int64_t nblocks, bool is32, int mode, bool inv) {
+  if (staged_eligible(a, is32, mode)) return inv ? launch_ntt_staged_inv32(a, mode) : launch_ntt_staged_fwd32(a, mode);
   if (inv) return is32 ? launch_ntt_pass_inv32(a, nblocks, mode) : launch_ntt_pass_inv64(a, nblocks, mode);
   if (a.gdec_power) return is32 ? launch_ntt_pass_fwd32_gdec(a, nblocks, mode) : launch_ntt_pass_fwd64_gdec(a, nblocks, mode);
   return is32 ? launch_ntt_pass_fwd32(a, nblocks, mode) : launch_ntt_pass_fwd64(a, nblocks, mode);

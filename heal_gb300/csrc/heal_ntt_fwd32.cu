@@ -7,6 +7,7 @@ namespace heal {
 int launch_ntt_batch_fwd32(const NttBatchArgs &b, int64_t nblocks, int mode, int p, int threads, size_t smem) {
   return launch_batch_direction<int32_t, false>(b, nblocks, mode, p, threads, smem);
 }
+int launch_ntt_staged_fwd32(const NttArgs &a, int mode) { return launch_staged_direction<int32_t, false>(a, mode); }
 int launch_ntt_pass_fwd32(const NttArgs &a, int64_t nblocks, int mode) {
   return launch_direction_typed<int32_t, false>(a, nblocks, mode);
 }

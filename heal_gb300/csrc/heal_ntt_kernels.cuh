@@ -6,7 +6,7 @@
 // every butterfly equals the reference's).
 //
 // Register-blocked form: each thread keeps 8 points (16 in the forward
-// canonical 32-bit mode) of one column in registers and runs up to 3 (4)
+// mode for q < 2^31) of one column in registers and runs up to 3 (4)
 // stages per step on them (a radix-8 / radix-16 group: every twiddle is loaded
 // once per group of butterflies that share it); between steps the points are
 // exchanged through a shared-memory tile.
@@ -88,7 +88,7 @@ struct Word<false> {
 };
 
 // Arithmetic modes of the register kernel:
-//   0  32-bit words, canonical values     (every q < 2^31)
+//   0  32-bit words, values in [0, 2q)    (every q < 2^31)
 //   1  32-bit words, Harvey's lazy ranges (every q < 2^30: 4q < 2^32)
 //   2  64-bit words, Harvey's lazy ranges (every q < 2^62: 4q < 2^64)
 //   3  64-bit words, growing ranges       (q < 2^57 forward, q < 2^(63 - P) inverse)
@@ -111,7 +111,7 @@ __host__ __device__ constexpr bool mode_wide(int mode) { return mode >= MODE_W64
 
 // log2 of the points one thread of the register kernel holds (a radix-2^lpt
 // step per shared-memory exchange): 16 points for the forward transform in
-// canonical 32-bit words, 8 otherwise (measured best for each: the 64-bit
+// mode 0 (32-bit words, q < 2^31), 8 otherwise (measured best for each: the 64-bit
 // modes need two registers per point, and the inverse and lazy 32-bit
 // kernels ran slower with 16)
 #ifndef HEAL_NTT_LPT
@@ -417,8 +417,9 @@ __device__ __forceinline__ int point_of(int step, int r, int e) {
 }
 
 // One register step: stages [kLPT*STEP, kLPT*STEP + qn) on the kPT >> qn
-// sets of 2^qn points this thread holds.
-template <int MODE, bool INV, int LOGP, int STEP>
+// sets of 2^qn points this thread holds.  TWS: the twiddle row is in shared
+// memory (the staged kernel), else read through the read-only cache.
+template <int MODE, bool INV, int LOGP, int STEP, bool TWS = false>
 __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[1 << lpt_of(MODE, INV)], int r, int64_t G,
                                          const typename Word<mode_wide(MODE)>::Pair *twp,
                                          typename Word<mode_wide(MODE)>::W q) {
@@ -445,7 +446,8 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
         const int dist = 1 << (qn - 1 - kk);
 #pragma unroll
         for (int gl = 0; gl < (1 << kk); ++gl) {
-          const Pair pr = __ldg(twp + (G << st) + ((int64_t)hi << kk) + gl);
+          const int64_t ti = (G << st) + ((int64_t)hi << kk) + gl;
+          const Pair pr = TWS ? twp[ti] : __ldg(twp + ti);
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
             const int a = base + gl * 2 * dist + off, b = a + dist;
@@ -460,13 +462,12 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
               const W tv = mulw_lazy<WIDE>(v[b], pr, q);
               v[a] = u + tv;
               v[b] = u - tv + q2;
-            } else {
-              const W tv = mulw<WIDE>(v[b], pr, q);
-              W nu = v[a] + tv;
-              nu = nu >= q ? nu - q : nu;
-              const W nv = v[a] >= tv ? v[a] - tv : v[a] + (q - tv);
-              v[a] = nu;
-              v[b] = nv;
+            } else {  // 32-bit words, values in [0, 2q) (q < 2^31: 2q < 2^32)
+              const W u = min(v[a], v[a] - q);        // [0, q): u - q wraps above u when u < q
+              W tv = mulw_lazy<WIDE>(v[b], pr, q);    // [0, 2q)
+              tv = min(tv, tv - q);
+              v[a] = u + tv;                          // [0, 2q)
+              v[b] = u - tv + q;                      // (0, 2q)
             }
           }
         }
@@ -476,7 +477,8 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
         const W qs = q << st;  // growing ranges: every value entering stage st is below 2^st q
 #pragma unroll
         for (int gl = 0; gl < (1 << (qn - 1 - kk)); ++gl) {
-          const Pair pr = __ldg(twp + G * (int64_t)(P >> (st + 1)) + ((int64_t)hi << (qn - 1 - kk)) + gl);
+          const int64_t ti = G * (int64_t)(P >> (st + 1)) + ((int64_t)hi << (qn - 1 - kk)) + gl;
+          const Pair pr = TWS ? twp[ti] : __ldg(twp + ti);
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
             const int a = base + gl * 2 * dist + off, b = a + dist;
@@ -490,12 +492,10 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
               const W d = v[a] - v[b] + q2;
               v[a] = s;
               v[b] = mulw_lazy<WIDE>(d, pr, q);
-            } else {
-              W nu = v[a] + v[b];
-              nu = nu >= q ? nu - q : nu;
-              const W d = v[a] >= v[b] ? v[a] - v[b] : v[a] + (q - v[b]);
-              v[a] = nu;
-              v[b] = mulw<WIDE>(d, pr, q);
+            } else {  // 32-bit words, values in [0, 2q)
+              const W u = min(v[a], v[a] - q), w = min(v[b], v[b] - q);  // [0, q)
+              v[a] = u + w;                                               // [0, 2q)
+              v[b] = mulw_lazy<WIDE>(u - w + q, pr, q);                   // [0, 2q)
             }
           }
         }
@@ -505,7 +505,7 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
 }
 
 // Steps STEP .. NSTEP-1, exchanging through the shared tile between steps.
-template <int MODE, bool INV, int LOGP, int STEP>
+template <int MODE, bool INV, int LOGP, int STEP, bool TWS = false>
 __device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)[1 << lpt_of(MODE, INV)], int r, int c, int logC,
                                           int64_t *tile, int64_t G,
                                           const typename Word<mode_wide(MODE)>::Pair *twp,
@@ -535,8 +535,8 @@ __device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)
       }
       __syncthreads();
     }
-    reg_step<MODE, INV, LOGP, STEP>(v, r, G, twp, q);
-    reg_steps<MODE, INV, LOGP, STEP + 1>(v, r, c, logC, tile, G, twp, q);
+    reg_step<MODE, INV, LOGP, STEP, TWS>(v, r, G, twp, q);
+    reg_steps<MODE, INV, LOGP, STEP + 1, TWS>(v, r, c, logC, tile, G, twp, q);
   }
 }
 
@@ -636,7 +636,8 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
   }
   reg_steps<MODE, INV, LOGP, 0>(v, r, c, logC, tile, x.G, twp, q);
 
-  // ---- back to canonical residues (forward values < 4q, inverse < 2q;
+  // ---- back to canonical residues (forward values < 4q, inverse < 2q,
+  // both < 2q in mode 0;
   // growing ranges: a Shoup product by 1, unless the m^-1 product follows or
   // the next pass takes the values as they are)
   if (MODE == MODE_W64_GROW) {
@@ -648,11 +649,11 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
         v[e] = u >= q ? u - q : u;
       }
     }
-  } else if (LAZY) {
+  } else {
 #pragma unroll
     for (int e = 0; e < kPT; ++e) {
       W u = v[e];
-      if (!INV) u = u >= q + q ? u - (q + q) : u;
+      if (LAZY && !INV) u = u >= q + q ? u - (q + q) : u;
       v[e] = u >= q ? u - q : u;
     }
   }

@@ -2,9 +2,56 @@
 // direction (included once by heal_ntt_fwd.cu and once by heal_ntt_inv.cu,
 // so the two directions compile in parallel).
 #pragma once
+#include <algorithm>
+
 #include "heal_ntt_kernels.cuh"
+#include "heal_ntt_staged.cuh"
 
 namespace heal {
+
+// ---------------------------------------------------------- staged kernel
+// One persistent launch of ntt_staged_kernel over the pass's tiles, at the
+// resident CTAs per SM the occupancy calculator gives.  The tile
+// decomposition is redone for the kernel's own tile width C.
+template <typename T, int MODE, bool INV, int LOGP, int C, int MINB>
+static int launch_staged_typed(const NttArgs &a0) {
+  typedef StagedShape<T, MODE, INV, LOGP, C, MINB> S;
+  static int per_sm = 0;
+  auto kern = ntt_staged_kernel<T, MODE, INV, LOGP, C, MINB>;
+  if (!per_sm) {
+    HEAL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BYTES));
+    int nb = 0;
+    HEAL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, S::THREADS, S::SMEM_BYTES));
+    per_sm = std::max(nb, 1);
+  }
+  NttArgs a = a0;
+  a.C = C;
+  a.logC = S::LOGC;
+  a.ngroups_t = (a.k + C - 1) / C;
+  a.fast_bid = a.ngroups_t < (int64_t)UINT32_MAX && a.l * a.r < (int64_t)UINT32_MAX && a.r < (int64_t)UINT32_MAX;
+  if (a.fast_bid) {
+    a.fd_groups = fastdiv_make((uint32_t)a.ngroups_t);
+    a.fd_nij = fastdiv_make((uint32_t)(a.l * a.r));
+    a.fd_r = fastdiv_make((uint32_t)a.r);
+  }
+  const int64_t ntiles = a.nsets * a.l * a.r * a.ngroups_t;
+  if (ntiles < 1 || ntiles > 0x7FFFFFFF) return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT: more than 2^31 - 1 tiles in one call");
+  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)per_sm * device_sm_count());
+  kern<<<(unsigned)grid, S::THREADS, S::SMEM_BYTES, stream()>>>(a, (uint32_t)ntiles);
+  return check_launch("ntt_staged_pass");
+}
+
+// the staged form (int32 tensors: 256-point passes in the 32-bit modes,
+// tiles of 8 limbs, 512 threads per SM)
+template <typename T, bool INV>
+static int launch_staged_direction(const NttArgs &a, int mode) {
+  if constexpr (sizeof(T) == 4) {
+    constexpr int C = 8;
+    if (mode == MODE_N32_LAZY) return launch_staged_typed<T, MODE_N32_LAZY, INV, 8, C, 2>(a);
+    if (mode == MODE_N32) return launch_staged_typed<T, MODE_N32, INV, 8, C, INV ? 2 : 4>(a);
+  }
+  return set_error(HEAL_ERR_RUNTIME, "NTT: no staged kernel for this element type and mode");
+}
 
 template <typename Kern>
 static int launch_with_smem(Kern kern, const NttArgs &a, int64_t nblocks, int threads, size_t smem, bool &attr_set) {

@@ -39,7 +39,8 @@ LIMBS = [0, 5, 13, 23]   # first and last tile, both ends of a 4-limb tile, a ti
 
 
 def oracle_parts(ch, ct, li):
-    """The oracle's INTT limbs, digit-transform columns and output limbs for limbs `li`."""
+    """The oracle's INTT limbs, the digit-transform columns times the key (the
+    chain multiplies them in place) and the output limbs, for limbs `li`."""
     h = ch.host
     li = np.asarray(li)
     x = O.intt(np.ascontiguousarray(ct[..., li]), h["p"][li], h["perm"], h["itw"][li], h["minv"][li])
@@ -48,8 +49,10 @@ def oracle_parts(ch, ct, li):
     n, k = ct.shape[1], len(li)
     p_t = np.repeat(h["p"][li], ch.D)
     dn = O.ntt(dig.reshape(2, n, 1, k * ch.D), p_t, h["perm"], np.repeat(h["tw"][li], ch.D, axis=0))
+    cols = (li[:, None] * ch.D + np.arange(ch.D)[None, :]).reshape(-1)
+    prod = O.modmul(dn, np.ascontiguousarray(h["key"][..., cols]), p_t)
     out = oracle_chain(h, ct, ch.D, ch.bits, limb_idx=li)
-    return x, dn, out
+    return x, prod, out
 
 
 def test_keyswitch_chain_full_shape_vs_oracle(chain):
@@ -58,10 +61,10 @@ def test_keyswitch_chain_full_shape_vs_oracle(chain):
     dct = capi.DeviceArray.from_numpy(ct)
     out = capi.DeviceArray.empty(ch.shape(), np.int64)
     ch.run(dct, out)
-    x_want, dn_want, out_want = oracle_parts(ch, ct, LIMBS)
+    x_want, prod_want, out_want = oracle_parts(ch, ct, LIMBS)
     cols = (np.asarray(LIMBS)[:, None] * ch.D + np.arange(ch.D)[None, :]).reshape(-1)
     assert np.array_equal(ch.x.numpy()[..., LIMBS], x_want), "INTT of [2, 65536, 1, 24] differs"
-    assert np.array_equal(ch.dn.numpy()[..., cols], dn_want), "digit NTT of [2, 65536, 1, 72] differs"
+    assert np.array_equal(ch.dn.numpy()[..., cols], prod_want), "digit NTT x key of [2, 65536, 1, 72] differs"
     got = out.numpy()
     assert np.array_equal(got[..., LIMBS], out_want), "keyswitch chain output differs"
     # the fused three-call form of the same chain
