@@ -976,7 +976,8 @@ def ntt_probe(args):
     """--mode ntt: one batched NTT alone, for ncu captures of the pass
     kernels.  --probe digits: [batch, 65536, 1, 72] int64 under the chain's
     50-bit primes tiled 3x (the digit tensor of batch/2 chains); --probe int32:
-    [batch, 65536, 1, 32] int32 under 31-bit primes; --probe ct-intt: the INTT
+    [batch, 65536, 1, 32] int32 under 31-bit primes (--probe int32-intt: its
+    INTT); --probe ct-intt: the INTT
     of [batch, 65536, 1, 24] int64 (the chain's ciphertext).  Prints one JSON
     line with the CUDA-event time per call."""
     import torch
@@ -986,8 +987,8 @@ def ntt_probe(args):
     heal_gb300.build()
     capi.check(capi.lib().heal_init(0))
     stream = torch.cuda.ExternalStream(capi.stream())
-    inverse = args.probe == "ct-intt"
-    if args.probe == "int32":
+    inverse = args.probe in ("ct-intt", "int32-intt")
+    if args.probe in ("int32", "int32-intt"):
         dt, k, qs = np.int32, 32, P.ntt_primes(1 << 31, N, 32)
         p_t, perm, tw_t, itw, minv = P.ntt_tables(qs, N, dt)
     elif inverse:
@@ -1043,7 +1044,7 @@ def main():
     ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--inflight", type=int, default=2, help="chains in flight on their own streams")
-    ap.add_argument("--probe", default="digits", choices=["digits", "int32", "ct-intt"])
+    ap.add_argument("--probe", default="digits", choices=["digits", "int32", "int32-intt", "ct-intt"])
     args = ap.parse_args()
     unknown = set(args.configs.split(",")) - set(WORKLOADS) - {""}
     if unknown:

@@ -255,9 +255,15 @@ __device__ __forceinline__ bool needs_exact(const NttArgs &g, int64_t x, int64_t
 
 // ---------------------------------------------------------- exact path
 // The tile (raw values, tidx layout) through the reference's arithmetic,
-// one stage per barrier; then stored (with m_inv scaling / gather).
-template <typename T, bool INV>
-__device__ __noinline__ void exact_tile(const NttArgs &g, const TileCtx &x, int64_t *tile) {
+// one stage per barrier; then stored (with m_inv scaling / gather).  TT is
+// the tile's word: int64, or the element type itself for int32 tensors
+// (each stage's results are truncated remainders by q < 2^31 and fit).
+// The tile is named by its index, not by its TileCtx: a context passed by
+// reference to this out-of-line function would be stored to local memory on
+// every tile of the fast path.
+template <typename T, bool INV, typename TT = int64_t>
+__device__ __noinline__ void exact_tile(const NttArgs &g, uint32_t block, TT *tile) {
+  const TileCtx x = tile_ctx(g, block);
   const int P = x.P, C = x.C, logC = x.logC, p = g.p;
   const bool is32 = sizeof(T) == 4;
   const int nbf = (P >> 1) * C;
@@ -294,8 +300,8 @@ __device__ __noinline__ void exact_tile(const NttArgs &g, const TileCtx &x, int6
         nu = crem128((i128)u + v, q);
         nv = crem128(((i128)u + q - v) * s, q);
       }
-      tile[tidx(su, c, logC)] = nu;
-      tile[tidx(sv, c, logC)] = nv;
+      tile[tidx(su, c, logC)] = (TT)nu;
+      tile[tidx(sv, c, logC)] = (TT)nv;
     }
     __syncthreads();
   }
@@ -303,7 +309,8 @@ __device__ __noinline__ void exact_tile(const NttArgs &g, const TileCtx &x, int6
     const int s = e >> logC, c = e & (C - 1);
     const int64_t t = x.t0 + c;
     if (t >= g.k) continue;
-    int64_t val = g.store_gather ? tile[tidx((int)perm_row(g, g.store_gather, s), c, logC)] : tile[tidx(s, c, logC)];
+    int64_t val = g.store_gather ? (int64_t)tile[tidx((int)perm_row(g, g.store_gather, s), c, logC)]
+                                 : (int64_t)tile[tidx(s, c, logC)];
     if (g.scale) val = crem128((i128)val * raw_any(g.minv_raw, t * g.minv_s0, is32), g.q[t]);
     store_point<T>(g, x, s, t, val);
   }
@@ -329,7 +336,7 @@ __global__ void __launch_bounds__(256) ntt_small_kernel(const __grid_constant__ 
   const bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
                      (g.scale && g.minv_neg && *g.minv_neg);
   if (exact) {
-    exact_tile<T, INV>(g, x, tile);
+    exact_tile<T, INV>(g, blockIdx.x, tile);
     return;
   }
   const int nbf = (P >> 1) * C;
@@ -418,15 +425,16 @@ __device__ __forceinline__ int point_of(int step, int r, int e) {
 
 // One register step: stages [kLPT*STEP, kLPT*STEP + qn) on the kPT >> qn
 // sets of 2^qn points this thread holds.  TWS: the twiddle row is in shared
-// memory (the staged kernel), else read through the read-only cache.
-template <int MODE, bool INV, int LOGP, int STEP, bool TWS = false>
-__device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[1 << lpt_of(MODE, INV)], int r, int64_t G,
+// memory (the staged kernel), else read through the read-only cache.  LPT:
+// log2 of the points per thread (the register kernel's lpt_of by default).
+template <int MODE, bool INV, int LOGP, int STEP, bool TWS = false, int LPT = lpt_of(MODE, INV)>
+__device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[1 << LPT], int r, int64_t G,
                                          const typename Word<mode_wide(MODE)>::Pair *twp,
                                          typename Word<mode_wide(MODE)>::W q) {
   constexpr bool WIDE = mode_wide(MODE);
   constexpr bool GROW = MODE == MODE_W64_GROW;
   constexpr bool LAZY = MODE != MODE_N32;
-  constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
+  constexpr int kLPT = LPT, kPT = 1 << kLPT;
   typedef typename Word<WIDE>::W W;
   typedef typename Word<WIDE>::Pair Pair;
   constexpr int P = 1 << LOGP;
@@ -475,12 +483,18 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
         const int hi = id >> st0;
         const int dist = 1 << kk;
         const W qs = q << st;  // growing ranges: every value entering stage st is below 2^st q
+        // one flat loop over the step's butterflies (group gl, offset off):
+        // nested gl / off loops were left partly rolled at 16 points per
+        // thread, which put v[] in local memory
+        Pair pr;
 #pragma unroll
-        for (int gl = 0; gl < (1 << (qn - 1 - kk)); ++gl) {
-          const int64_t ti = G * (int64_t)(P >> (st + 1)) + ((int64_t)hi << (qn - 1 - kk)) + gl;
-          const Pair pr = TWS ? twp[ti] : __ldg(twp + ti);
-#pragma unroll
-          for (int off = 0; off < dist; ++off) {
+        for (int j = 0; j < (1 << (qn - 1)); ++j) {
+          const int gl = j >> kk, off = j & (dist - 1);
+          if (off == 0) {
+            const int64_t ti = G * (int64_t)(P >> (st + 1)) + ((int64_t)hi << (qn - 1 - kk)) + gl;
+            pr = TWS ? twp[ti] : __ldg(twp + ti);
+          }
+          {
             const int a = base + gl * 2 * dist + off, b = a + dist;
             if (GROW) {
               const W d = v[a] - v[b] + qs;
@@ -505,13 +519,13 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
 }
 
 // Steps STEP .. NSTEP-1, exchanging through the shared tile between steps.
-template <int MODE, bool INV, int LOGP, int STEP, bool TWS = false>
-__device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)[1 << lpt_of(MODE, INV)], int r, int c, int logC,
+template <int MODE, bool INV, int LOGP, int STEP, bool TWS = false, int LPT = lpt_of(MODE, INV)>
+__device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)[1 << LPT], int r, int c, int logC,
                                           int64_t *tile, int64_t G,
                                           const typename Word<mode_wide(MODE)>::Pair *twp,
                                           typename Word<mode_wide(MODE)>::W q) {
   typedef typename Word<mode_wide(MODE)>::W W;
-  constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
+  constexpr int kLPT = LPT, kPT = 1 << kLPT;
   constexpr int NSTEP = (LOGP + kLPT - 1) / kLPT;
   if constexpr (STEP < NSTEP) {
     if constexpr (STEP > 0) {
@@ -535,8 +549,8 @@ __device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)
       }
       __syncthreads();
     }
-    reg_step<MODE, INV, LOGP, STEP, TWS>(v, r, G, twp, q);
-    reg_steps<MODE, INV, LOGP, STEP + 1, TWS>(v, r, c, logC, tile, G, twp, q);
+    reg_step<MODE, INV, LOGP, STEP, TWS, LPT>(v, r, G, twp, q);
+    reg_steps<MODE, INV, LOGP, STEP + 1, TWS, LPT>(v, r, c, logC, tile, G, twp, q);
   }
 }
 
@@ -621,7 +635,7 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
       tile[tidx(point_of<INV, LOGP, kLPT>(0, r, e), c, logC)] = w;
     }
     __syncthreads();
-    exact_tile<T, INV>(g, x, tile);
+    exact_tile<T, INV>(g, block, tile);
     return;
   }
 

@@ -11,8 +11,9 @@ namespace heal {
 
 // ---------------------------------------------------------- staged kernel
 // One persistent launch of ntt_staged_kernel over the pass's tiles, at the
-// resident CTAs per SM the occupancy calculator gives.  The tile
-// decomposition is redone for the kernel's own tile width C.
+// resident CTAs per SM the occupancy calculator gives (rounded to whole
+// shares of every limb group).  The tile decomposition is redone for the
+// kernel's own tile width C.
 template <typename T, int MODE, bool INV, int LOGP, int C, int MINB>
 static int launch_staged_typed(const NttArgs &a0) {
   typedef StagedShape<T, MODE, INV, LOGP, C, MINB> S;
@@ -34,21 +35,26 @@ static int launch_staged_typed(const NttArgs &a0) {
     a.fd_nij = fastdiv_make((uint32_t)(a.l * a.r));
     a.fd_r = fastdiv_make((uint32_t)a.r);
   }
-  const int64_t ntiles = a.nsets * a.l * a.r * a.ngroups_t;
-  if (ntiles < 1 || ntiles > 0x7FFFFFFF) return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT: more than 2^31 - 1 tiles in one call");
-  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)per_sm * device_sm_count());
-  kern<<<(unsigned)grid, S::THREADS, S::SMEM_BYTES, stream()>>>(a, (uint32_t)ntiles);
+  const int64_t nunits = a.nsets * a.l * a.r;  // tiles per limb group
+  if (nunits < 1 || nunits * a.ngroups_t > 0x7FFFFFFF)
+    return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT: more than 2^31 - 1 tiles in one call");
+  // every limb group gets the same number of CTAs (shares), each a contiguous run of its tiles
+  const int64_t shares =
+      std::max<int64_t>(1, std::min<int64_t>(nunits, (int64_t)per_sm * device_sm_count() / a.ngroups_t));
+  const int64_t grid = shares * a.ngroups_t;
+  if (grid > 0x7FFFFFFF) return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT: too many limb groups in one call");
+  kern<<<(unsigned)grid, S::THREADS, S::SMEM_BYTES, stream()>>>(a, (uint32_t)nunits);
   return check_launch("ntt_staged_pass");
 }
 
 // the staged form (int32 tensors: 256-point passes in the 32-bit modes,
-// tiles of 8 limbs, 512 threads per SM)
+// tiles of 8 limbs, 16 points per thread: 128-thread CTAs, 4 per SM)
 template <typename T, bool INV>
 static int launch_staged_direction(const NttArgs &a, int mode) {
   if constexpr (sizeof(T) == 4) {
     constexpr int C = 8;
-    if (mode == MODE_N32_LAZY) return launch_staged_typed<T, MODE_N32_LAZY, INV, 8, C, 2>(a);
-    if (mode == MODE_N32) return launch_staged_typed<T, MODE_N32, INV, 8, C, INV ? 2 : 4>(a);
+    if (mode == MODE_N32_LAZY) return launch_staged_typed<T, MODE_N32_LAZY, INV, 8, C, 4>(a);
+    if (mode == MODE_N32) return launch_staged_typed<T, MODE_N32, INV, 8, C, 4>(a);
   }
   return set_error(HEAL_ERR_RUNTIME, "NTT: no staged kernel for this element type and mode");
 }
