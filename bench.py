@@ -57,7 +57,7 @@ CONFIG = {"workload": "keyswitch chain: ct[2][24][65536] int64, 50-bit NTT prime
 CHAINS_PER_STEP = CONFIG["chains_per_step"]
 RING = 8
 # the workloads reported under "configs" beside the headline (--configs)
-WORKLOADS = ("roundtrip", "ragged", "int32_ntt", "serving")
+WORKLOADS = ("roundtrip", "ragged", "ragged_keyswitch", "int32_ntt", "serving")
 
 
 def dist_info():
@@ -595,6 +595,8 @@ def other_configs(args, timed, stream):
         out["int32_ntt_n65536"] = int32_ntt_config(args, timed)
     if "ragged" in want:
         out["ragged_256"] = ragged_config(args, timed)
+    if "ragged_keyswitch" in want:
+        out["ragged_keyswitch_256"] = ragged_keyswitch_config(args, timed)
     if "serving" in want:
         out["serving"] = serving_config(args)
     return out
@@ -822,6 +824,68 @@ def ragged_config(args, timed):
             "autotuned_shapes": len(shapes), "autotune_s": tune_s, "setup_s": setup_s,
             "plans_sample": {f"{n}x{l}": {"fwd": plans[(n, l)][0], "inv": plans[(n, l)][1]}
                              for n, l in shapes[:: max(1, len(shapes) // 6)]}}
+
+
+def ragged_keyswitch_config(args, timed):
+    """Ragged keyswitch: the fused keyswitch step (INTT, g_decomposition + NTT of
+    the digits, modmul -> axis_modsum -> permute) of 256 ciphertexts of mixed
+    ring degree and limb count, as the plain loop of three calls per
+    ciphertext, as that loop captured in one CUDA graph, and as one
+    heal_keyswitch_batch launch; the same on 256 small-ring ciphertexts
+    (N in 2^12, 2^13), where launch costs dominate."""
+    import gc
+    from heal_gb300 import capi
+    from heal_gb300.configs import RaggedKeyswitch
+    from oracle.chain import oracle_chain
+    hbm, _ = peaks()
+    res = {"workload": "256 ciphertexts [2, N, 1, L] int64, N in 2^12..2^16, L uniform in 2..32, 50-bit primes; "
+                       "intt -> g_decomposition (D=3, base 2^17) + ntt of the digits -> modmul(key) -> "
+                       "axis_modsum(digits) -> permute(X->X^5) per ciphertext"}
+    for name, kw in (("mixed", {}), ("small_rings", {"logns": (12, 13), "lmax": 16})):
+        t0 = time.time()
+        rk = RaggedKeyswitch(**kw)
+        setup_s = time.time() - t0
+        rk.run()
+        want = [o.numpy() for o in rk.outs]
+        steps = max(5, args.steps // 4)
+        for _ in range(2):
+            rk.run()
+        ms_loop, l_loop = timed(lambda s: rk.run(), steps)
+        g = capi.Graph(rk.run)
+        for _ in range(2):
+            g.launch()
+        ms_graph, l_graph = timed(lambda s: g.launch(), steps)
+        del g
+        for _ in range(2):
+            rk.run_batched()
+        ms_batch, l_batch = timed(lambda s: rk.run_batched(), steps)
+        equal = all(np.array_equal(o.numpy(), w) for o, w in zip(rk.outs, want))
+        # the oracle on the two smallest ciphertexts
+        small = sorted(range(len(rk.specs)), key=lambda i: rk.specs[i][0] * rk.specs[i][1])[:2]
+        oracle_equal = all(np.array_equal(want[i], oracle_chain(rk.host_tables(i), rk.host_cts[i], rk.D, rk.BITS))
+                           for i in small)
+        best = ms_batch / steps
+        r = {"ring_degrees": {str(n): sum(1 for m, _ in rk.specs if m == n) for n in sorted({n for n, _ in rk.specs})},
+             "step_ms_loop": ms_loop / steps, "step_ms_graph": ms_graph / steps, "step_ms_persistent": best,
+             "launches_per_step_loop": l_loop / steps, "launches_per_step_persistent": l_batch / steps,
+             "persistent_vs_loop": ms_loop / ms_batch, "persistent_vs_graph": ms_graph / ms_batch,
+             "ciphertexts_per_s_persistent": len(rk.specs) / (best / 1e3),
+             "persistent_equals_loop": equal, "oracle_equal": {"ciphertexts_checked": len(small), "equal": oracle_equal},
+             "roofline": hbm_roofline(rk.bytes_per_step(), best, "heal_keyswitch_batch (one persistent launch)"),
+             "setup_s": setup_s}
+        if name == "mixed":
+            i0 = small[0]
+            cpu_s, runs, threads = cpu_run(lambda: oracle_chain(rk.host_tables(i0), rk.host_cts[i0], rk.D, rk.BITS),
+                                           3.0)
+            n0, l0 = rk.specs[i0]
+            scale = rk.bytes_per_step() / (2 * n0 * l0 * 8 * (2 + 4 + 7))
+            r["cpu_baseline"] = {"value": len(rk.specs) / (cpu_s * scale), "unit": "ciphertexts/s", "cores": threads,
+                                 "kind": "port", "sample": f"the oracle chain on one ciphertext (N={n0}, L={l0}, "
+                                                           f"{runs} runs), scaled to the batch by algorithmic bytes"}
+        res[name] = r
+        del rk
+        gc.collect()
+    return res
 
 
 def serving_config(args, count: int = 4000, rate: float = 2000.0):

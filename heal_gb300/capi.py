@@ -32,6 +32,15 @@ class NttJob(ctypes.Structure):
                 ("result", Tensor)]
 
 
+class KeyswitchJob(ctypes.Structure):
+    """heal_keyswitch_job: one fused keyswitch step of a heal_keyswitch_batch call."""
+    _fields_ = [("ct", Tensor), ("p", Tensor), ("perm", Tensor), ("inv_twiddles", Tensor), ("m_inv", Tensor),
+                ("x", Tensor), ("power", ctypes.c_int64), ("base_bits", ctypes.c_int64), ("p_digits", Tensor),
+                ("twiddles_digits", Tensor), ("digits", Tensor), ("tail_a", Tensor), ("tail_b", Tensor),
+                ("tail_axis", ctypes.c_int64), ("galois", Tensor), ("elementwise_axis", ctypes.c_int64),
+                ("perm_axis", ctypes.c_int64), ("result", Tensor)]
+
+
 _P = ctypes.POINTER(Tensor)
 _I64, _U64, _I32, _VP, _SZ = ctypes.c_int64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t
 SIGNATURES = {
@@ -89,6 +98,7 @@ SIGNATURES = {
     "heal_g_decomposition_ntt": ([_P, _I64, _I64, _P, _P, _P, _P], ctypes.c_int),
     "heal_ntt_butterfly_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "heal_ntt_batch": ([ctypes.c_int, ctypes.POINTER(NttJob), _I64], ctypes.c_int),
+    "heal_keyswitch_batch": ([ctypes.POINTER(KeyswitchJob), _I64], ctypes.c_int),
     "heal_ntt_set_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "heal_ntt_get_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.POINTER(ctypes.c_int),
                            ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
@@ -270,6 +280,22 @@ def ntt_jobs(jobs) -> "ctypes.Array":
 def ntt_batch(inverse: bool, jobs):
     """heal_ntt_batch over (a, p, perm, twiddles, m_inv or None, result) tuples."""
     check(lib().heal_ntt_batch(int(bool(inverse)), ntt_jobs(jobs), len(jobs)))
+
+
+def keyswitch_jobs(jobs) -> "ctypes.Array":
+    """heal_keyswitch_job array from dicts of DeviceArrays and integers keyed
+    by the struct's field names; the caller keeps the arrays alive."""
+    arr = (KeyswitchJob * max(1, len(jobs)))()
+    for i, j in enumerate(jobs):
+        for name, _ in KeyswitchJob._fields_:
+            v = j[name]
+            setattr(arr[i], name, v.desc() if isinstance(v, DeviceArray) else int(v))
+    return arr
+
+
+def keyswitch_batch(jobs):
+    """heal_keyswitch_batch over keyswitch job dicts (see keyswitch_jobs)."""
+    check(lib().heal_keyswitch_batch(keyswitch_jobs(jobs), len(jobs)))
 
 
 def synchronize():

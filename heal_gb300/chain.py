@@ -100,6 +100,15 @@ class KeyswitchChain:
         capi.call("heal_g_decomposition_ntt", self.x, self.D, self.bits, d["p_t"], d["perm"], d["tw_t"], self.dn)
         capi.call("heal_modmul_axis_sum_permute", self.prod_moved, self.key_moved, d["p"], 3, d["gal"], 2, 1, out)
 
+    def job(self, ct: capi.DeviceArray, out: capi.DeviceArray) -> dict:
+        """run_fused's three calls as one heal_keyswitch_batch job (fields of
+        capi.KeyswitchJob), on this chain's tables, key and intermediates."""
+        d = self.dev
+        return {"ct": ct, "p": d["p"], "perm": d["perm"], "inv_twiddles": d["itw"], "m_inv": d["minv"], "x": self.x,
+                "power": self.D, "base_bits": self.bits, "p_digits": d["p_t"], "twiddles_digits": d["tw_t"],
+                "digits": self.dn, "tail_a": self.prod_moved, "tail_b": self.key_moved, "tail_axis": 3,
+                "galois": d["gal"], "elementwise_axis": 2, "perm_axis": 1, "result": out}
+
     def bytes_per_chain_fused(self) -> int:
         """Algorithmic bytes of run_fused: the INTT's read and write, the
         digit NTT's read of x and write of the digit transforms, and one read

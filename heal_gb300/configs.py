@@ -247,3 +247,97 @@ class RaggedBatch:
     def bytes_per_step(self) -> int:
         """Algorithmic bytes of one pass over the batch."""
         return sum(self.bytes_of(i) for i in range(len(self.specs)))
+
+
+class RaggedKeyswitch:
+    """Ragged keyswitch batch: `count` ciphertexts [2, N_i, 1, L_i] int64 with
+    N_i drawn from 2^logns and L_i uniform in lmin..lmax, under the largest
+    50-bit primes q = 1 (mod 2 N_i) (limb t of every ciphertext of ring
+    degree N uses the t-th such prime), each through the fused keyswitch step
+    of heal_gb300.chain.KeyswitchChain (INTT, g_decomposition into D = 3
+    digits of base 2^17 with the NTT of the digits, then modmul by a key,
+    axis_modsum over the digits and the Galois permutation X -> X^5).  The
+    tables and the key of each ring degree cover lmax limbs; a ciphertext of
+    L limbs uses views of their first L limbs.  Runs as the plain loop of
+    three C-ABI calls per ciphertext, or as one heal_keyswitch_batch call."""
+
+    COUNT, LOGNS, LMIN, LMAX, D, BITS, BOUND = 256, (12, 13, 14, 15, 16), 2, 32, 3, 17, 1 << 50
+
+    def __init__(self, count: int = COUNT, logns=LOGNS, lmin: int = LMIN, lmax: int = LMAX, seed: int = 707):
+        idx = P.uniform(seed, (count,), 0, len(logns))
+        ls = P.uniform(seed + 1, (count,), lmin, lmax + 1)
+        self.specs = [(1 << int(logns[i]), int(l)) for i, l in zip(idx, ls)]
+        self.lmax, D = lmax, self.D
+        Dv, E = capi.DeviceArray.from_numpy, capi.DeviceArray.empty
+        self.qs, self.tabs = {}, {}
+        for n in sorted({n for n, _ in self.specs}):
+            qs = P.ntt_primes(self.BOUND, n, lmax)
+            p, perm, tw, itw, minv = P.ntt_tables(qs, n)
+            self.qs[n] = qs
+            host = {"p": p, "perm": perm, "tw": tw, "itw": itw, "minv": minv, "p_t": np.repeat(p, D),
+                    "tw_t": np.repeat(tw, D, axis=0),
+                    "key": P.residues(seed + n, (2, n, 1, lmax * D), np.repeat(p, D)),
+                    "gal": P.galois_perm(n, 5).reshape(1, n)}
+            self.tabs[n] = {"host": host, "dev": {k: Dv(v) for k, v in host.items()}}
+        self.cts, self.outs, self.jobs, self.host_cts = [], [], [], []
+        for i, (n, l) in enumerate(self.specs):
+            ct = P.residues(seed * 1000 + i, (2, n, 1, l), self.qs[n][:l])
+            self.host_cts.append(ct)
+            self.cts.append(Dv(ct))
+            self.outs.append(E((2, n, 1, l), np.int64))
+            self.jobs.append(self._job(i, E))
+
+    def _job(self, i, E) -> dict:
+        n, l = self.specs[i]
+        D, L = self.D, self.lmax
+        t = self.tabs[n]["dev"]
+        V = lambda arr, shape, strides, off=0: capi.DeviceArray(arr.buf, np.int64, shape, strides, arr.offset + off)
+        x = E((2, n, 1, l), np.int64, zero=False)
+        dn = E((2, n, 1, l * D), np.int64, zero=False)
+        key = t["key"]  # [2, n, 1, L * D]: the first l * D columns, viewed [2, n, 1, D, l] as in the chain
+        return {"ct": self.cts[i], "p": V(t["p"], (l,), (1,)), "perm": t["perm"],
+                "inv_twiddles": V(t["itw"], (l, n), (n, 1)), "m_inv": V(t["minv"], (l,), (1,)), "x": x,
+                "power": D, "base_bits": self.BITS, "p_digits": V(t["p_t"], (l * D,), (1,)),
+                "twiddles_digits": V(t["tw_t"], (l * D, n), (n, 1)), "digits": dn,
+                "tail_a": V(dn, (2, n, 1, D, l), (n * l * D, l * D, l * D, 1, D)),
+                "tail_b": V(key, (2, n, 1, D, l), (n * L * D, L * D, L * D, 1, D)),
+                "tail_axis": 3, "galois": t["gal"], "elementwise_axis": 2, "perm_axis": 1,
+                "result": self.outs[i]}
+
+    def run_calls(self, i: int):
+        """Ciphertext i's step as its three C-ABI calls."""
+        j = self.jobs[i]
+        capi.call("heal_intt", j["ct"], j["p"], j["perm"], j["inv_twiddles"], j["m_inv"], None, None, j["x"])
+        capi.call("heal_g_decomposition_ntt", j["x"], j["power"], j["base_bits"], j["p_digits"], j["perm"],
+                  j["twiddles_digits"], j["digits"])
+        capi.call("heal_modmul_axis_sum_permute", j["tail_a"], j["tail_b"], j["p"], j["tail_axis"], j["galois"],
+                  j["elementwise_axis"], j["perm_axis"], j["result"])
+
+    def run(self):
+        """The plain loop: three calls per ciphertext."""
+        for i in range(len(self.specs)):
+            self.run_calls(i)
+
+    def run_batched(self):
+        """Every ciphertext's step in one heal_keyswitch_batch call."""
+        if not hasattr(self, "_arr"):
+            self._arr = capi.keyswitch_jobs(self.jobs)
+        capi.check(capi.lib().heal_keyswitch_batch(self._arr, len(self.jobs)))
+
+    def host_tables(self, i: int) -> dict:
+        """Ciphertext i's tables and key as numpy arrays (the oracle chain's input)."""
+        n, l = self.specs[i]
+        h, D, L = self.tabs[n]["host"], self.D, self.lmax
+        cols = np.arange(l * D)
+        return {"p": h["p"][:l], "perm": h["perm"], "tw": h["tw"][:l], "itw": h["itw"][:l], "minv": h["minv"][:l],
+                "key": np.ascontiguousarray(h["key"][..., cols]), "gal": h["gal"]}
+
+    def bytes_per_step(self) -> int:
+        """Algorithmic bytes of the fused step over the batch (as
+        KeyswitchChain.bytes_per_chain_fused per ciphertext)."""
+        tot = 0
+        for n, l in self.specs:
+            ct = 2 * n * l * 8
+            dg = ct * self.D
+            tot += 2 * ct + (ct + dg) + (2 * dg + ct)
+        return tot

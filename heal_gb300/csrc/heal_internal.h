@@ -57,6 +57,7 @@ constexpr int kDiagRecords = 32;
 struct Diag {
   unsigned long long count;  // total events
   unsigned long long zero_mod;
+  unsigned long long wait_timeouts;  // dependency waits of heal_keyswitch_batch that ran out
   DiagRecord rec[kDiagRecords];
 };
 Diag *diag_device();

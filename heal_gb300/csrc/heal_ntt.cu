@@ -41,6 +41,7 @@
 
 #include "heal_internal.h"
 #include "heal_ntt_kernels.cuh"
+#include "heal_ntt_record.h"
 
 namespace heal {
 
@@ -114,6 +115,8 @@ struct NttDeferred {
 };
 struct NttCollector {
   bool validate_only = false;
+  bool record_all = false;  // ntt_record: every pass is recorded, none launched
+  int force_first_log = 0;  // ntt_record: the two-pass split to use (0: the plan's)
   std::vector<NttDeferred> passes;
   size_t job_begin = 0;  // first recorded pass of the transform being prepared
   int job_phase = 0;
@@ -147,6 +150,10 @@ static bool batchable(const NttArgs &a, int mode, bool inv) {
 static int launch_any(const NttArgs &a, int64_t nblocks, bool is32, int mode, bool inv) {
   if (NttCollector *col = t_collect) {
     const int phase = col->job_phase++;
+    if (col->record_all) {
+      col->passes.push_back(NttDeferred{phase, a, nblocks, mode, is32, inv});
+      return HEAL_OK;
+    }
     if (batchable(a, mode, inv)) {
       col->passes.push_back(NttDeferred{phase, a, nblocks, mode, is32, inv});
       return HEAL_OK;
@@ -329,7 +336,13 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
   // moduli >= 2^62 do not fit the 64-bit lazy ranges
   base.force_exact = m == 1 || mi.max_q >= (int64_t(1) << 62);
   const bool is32 = dt == HEAL_INT32;
-  const NttPlan plan = plan_for(dt, inv, logm, k);
+  NttPlan plan = plan_for(dt, inv, logm, k);
+  if (t_collect && t_collect->force_first_log) {
+    const int f = t_collect->force_first_log;
+    if (f < 1 || f > kSinglePassLogMax || logm - f < 1 || logm - f > kSinglePassLogMax)
+      return set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT: no two-pass split of this length at the requested point");
+    plan.first_log = f;
+  }
   int C = plan.tile_limbs;
   while (C > 1 && C / 2 >= k) C /= 2;
   int rc = HEAL_OK;
@@ -414,6 +427,8 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
           set_strides(y.ds, *res);
           y.store_scatter = pi.inv32;
           rc = launch_any(y, nb, is32, m2, false);
+        } else if (t_collect && t_collect->record_all) {
+          rc = set_error(HEAL_ERR_INVALID_ARGUMENT, "NTT: a permutation that is not a bijection cannot be recorded");
         } else {
           heal_tensor T2 = T1;
           rc = scratch_alloc((size_t)s * elem_size(dt), &tmp2);
@@ -470,6 +485,22 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
   return rc;
 }
 
+
+int ntt_record(bool inv, const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm, const heal_tensor *tw,
+               const heal_tensor *minv, const heal_tensor *res, int64_t gdec_power, int64_t gdec_bits, int first_log,
+               std::vector<NttRecorded> *out, std::vector<void *> *release) {
+  if (t_collect) return set_error(HEAL_ERR_RUNTIME, "NTT: already recording on this thread");
+  NttCollector col;
+  col.record_all = true;
+  col.force_first_log = first_log;
+  t_collect = &col;
+  const GdecSpec gd{gdec_power, gdec_bits};
+  const int rc = ntt_run(inv, a, p, perm, tw, minv, res, gdec_power ? &gd : nullptr);
+  t_collect = nullptr;
+  for (const NttDeferred &d : col.passes) out->push_back(NttRecorded{d.args, d.nblocks, d.mode, d.inv, d.is32});
+  release->insert(release->end(), col.release.begin(), col.release.end());
+  return rc;
+}
 
 // the recorded passes of a batch, launched per class (element type, mode,
 // direction, pass length, tile width), kNttBatch passes per launch

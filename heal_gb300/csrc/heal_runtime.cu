@@ -138,13 +138,15 @@ void mark_written(const void *p) {
 }
 
 // ============================================================ diagnostics
-static void flush_diag() {
-  if (!g_rt.ready) return;
+// Prints the warnings recorded on the device since the last flush; returns
+// HEAL_ERR_RUNTIME when a heal_keyswitch_batch dependency wait ran out.
+static int flush_diag() {
+  if (!g_rt.ready) return HEAL_OK;
   Diag h;
   if (cudaMemcpyAsync(&h, g_rt.diag, sizeof(Diag), cudaMemcpyDeviceToHost, stream()) != cudaSuccess ||
       cudaStreamSynchronize(stream()) != cudaSuccess)
-    return;
-  if (h.count == 0 && h.zero_mod == 0) return;
+    return HEAL_OK;
+  if (h.count == 0 && h.zero_mod == 0 && h.wait_timeouts == 0) return HEAL_OK;
   unsigned long long shown = std::min<unsigned long long>(h.count, kDiagRecords);
   for (unsigned long long i = 0; i < shown; ++i) {
     const DiagRecord &r = h.rec[i];
@@ -161,6 +163,10 @@ static void flush_diag() {
             h.zero_mod);
   cudaMemsetAsync(g_rt.diag, 0, sizeof(Diag), stream());
   cudaStreamSynchronize(stream());
+  if (h.wait_timeouts)
+    return set_error(HEAL_ERR_RUNTIME, "heal_keyswitch_batch: " + std::to_string(h.wait_timeouts) +
+                                           " dependency waits ran out; the results of that batch are incomplete");
+  return HEAL_OK;
 }
 
 // ================================================================ helpers
@@ -987,8 +993,7 @@ int heal_synchronize(void) {
   HEAL_CHECK(ensure_init());
   if (g_rt.capturing) return refuse_sync("heal_synchronize");
   HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
-  flush_diag();
-  return HEAL_OK;
+  return flush_diag();
 }
 
 void *heal_get_stream(void) {
@@ -1062,8 +1067,7 @@ int heal_d2h(void *dst, const void *src, size_t bytes) {
   if (g_rt.capturing) return refuse_sync("heal_d2h");
   if (bytes) HEAL_TRY_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, stream()));
   HEAL_TRY_CUDA(cudaStreamSynchronize(stream()));
-  flush_diag();
-  return HEAL_OK;
+  return flush_diag();
 }
 
 int heal_h2d_async(void *dst, const void *src, size_t bytes) {

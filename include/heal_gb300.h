@@ -299,6 +299,37 @@ typedef struct heal_ntt_job {
 } heal_ntt_job;
 int heal_ntt_batch(int inverse, const heal_ntt_job *jobs, int64_t count);
 
+/* Many fused keyswitch steps, of any ring degree 2^12 .. 2^16 and limb
+ * count, in one persistent launch (an extension: HEAL has no such op; each
+ * step is the composition of HEAL's intt, g_decomposition, ntt, modmul,
+ * axis_modsum and permute, example_impl/ntt_impl.cpp:69-170,
+ * g_decomposition_impl.cpp:10-67, modop_impl.cpp:44-101,
+ * axis_modsum_impl.cpp:12-76, permute_impl.cpp:8-65).  Job i is the three
+ * calls
+ *   heal_intt(ct, p, perm, inv_twiddles, m_inv, NULL, NULL, x)
+ *   heal_g_decomposition_ntt(x, power, base_bits, p_digits, perm, twiddles_digits, digits)
+ *   heal_modmul_axis_sum_permute(tail_a, tail_b, p, tail_axis, galois, elementwise_axis, perm_axis, result)
+ * and the results are bit-identical to making them job after job.  Every
+ * job is validated, with those calls' errors, before anything is enqueued;
+ * beyond them: int64 tensors, moduli below 2^55 (the transforms' 64-bit
+ * growing ranges), the bit-reversal permutation, a tail that takes the lean
+ * kernel (at most 4 terms), at most 256 jobs, and no job writing (x, digits,
+ * result) memory another job uses.  Tiles of all stages of all jobs run in
+ * one kernel whose waits on the previous stage of the same job are bounded;
+ * a wait that runs out makes the next heal_synchronize return
+ * HEAL_ERR_RUNTIME.  Not allowed while a graph is being captured. */
+typedef struct heal_keyswitch_job {
+  heal_tensor ct, p, perm, inv_twiddles, m_inv, x;
+  int64_t power, base_bits;
+  heal_tensor p_digits, twiddles_digits, digits;
+  heal_tensor tail_a, tail_b;
+  int64_t tail_axis;
+  heal_tensor galois;
+  int64_t elementwise_axis, perm_axis;
+  heal_tensor result;
+} heal_keyswitch_job;
+int heal_keyswitch_batch(const heal_keyswitch_job *jobs, int64_t count);
+
 /* The head of a keyswitch's digit transform in one call (an extension: HEAL
  * has no such op).  Defined as the composition of HEAL's own calls
  *   result = ntt(reshape(g_decomposition(a, power, base_bits),
