@@ -99,6 +99,7 @@ SIGNATURES = {
     "heal_ntt_butterfly_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "heal_ntt_batch": ([ctypes.c_int, ctypes.POINTER(NttJob), _I64], ctypes.c_int),
     "heal_keyswitch_batch": ([ctypes.POINTER(KeyswitchJob), _I64], ctypes.c_int),
+    "heal_keyswitch_batch_test_wait": ([ctypes.c_uint32, ctypes.c_int], ctypes.c_int),
     "heal_ntt_set_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "heal_ntt_get_plan": ([ctypes.c_int, ctypes.c_int, _I64, _I64, ctypes.POINTER(ctypes.c_int),
                            ctypes.POINTER(ctypes.c_int)], ctypes.c_int),

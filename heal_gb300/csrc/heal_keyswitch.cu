@@ -57,6 +57,7 @@ struct KsStage {
   uint32_t first;   // its first item in the queue
   uint32_t ntiles;  // its items
   int32_t dep;      // the stage whose items must all have finished first (-1: none)
+  uint32_t hold;    // items of dep beyond its own that the wait also needs (0; the test hook sets 1)
   int32_t kind;     // KS_* | pass length (log2) << 4 | (tail: terms << 8 | 32-bit perms << 12)
   union {
     NttArgs ntt;
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(kKsThreads, 8)
           const int s = ks_find(stages, nstages, cur < 0 ? 0 : cur, item);
           const int dep = stages[s].dep;
           if (ok && dep >= 0) {
-            const uint32_t need = stages[dep].ntiles;
+            const uint32_t need = stages[dep].ntiles + stages[s].hold;
             for (uint32_t it = 0; ld_acquire(done + dep) < need; ++it) {
               if (*abort_flag) {
                 ok = 0;
@@ -216,6 +217,9 @@ __global__ void __launch_bounds__(kKsThreads, 8)
 }
 
 // ------------------------------------------------------------------ host
+// the failure-path test hook (heal_keyswitch_batch_test_wait)
+static uint32_t g_ks_spin_limit = 1u << 22;  // about a second of polling (256 ns sleeps)
+static int g_ks_stall = 0;
 // the recorded call's own status and message, prefixed with the job
 static int ks_fail(int code, int64_t job, const char *what) {
   const std::string msg = heal_last_error();
@@ -337,7 +341,11 @@ static int ks_chunk(const heal_keyswitch_job *jobs, int64_t n, int64_t base) {
   }
   // a stage with no tiles (an empty result) counts as finished at once
   for (int64_t j = 0; j < n; ++j)
-    for (int k = 0; k < 5; ++k) stages[where[j * 5 + k]].dep = k ? where[j * 5 + k - 1] : -1;
+    for (int k = 0; k < 5; ++k) {
+      KsStage &st = stages[where[j * 5 + k]];
+      st.dep = k ? where[j * 5 + k - 1] : -1;
+      st.hold = g_ks_stall && k == 4 ? 1u : 0u;  // the test hook: the tails wait for a tile that never comes
+    }
   const int nst = (int)stages.size();
   void *dstages = nullptr, *state = nullptr;
   rc = scratch_alloc(sizeof(KsStage) * stages.size(), &dstages);
@@ -358,8 +366,7 @@ static int ks_chunk(const heal_keyswitch_job *jobs, int64_t n, int64_t base) {
       per_sm = std::max(nb, 1);
     }
     const int64_t grid = std::min<int64_t>((int64_t)items, (int64_t)per_sm * device_sm_count());
-    // about a second of polling (256 ns sleeps) before a wait gives up
-    const uint32_t spin_limit = 1u << 22;
+    const uint32_t spin_limit = g_ks_spin_limit;
     keyswitch_batch_kernel<<<(unsigned)grid, kKsThreads, (size_t)8 * kKsThreads * sizeof(int64_t), stream()>>>(
         (const KsStage *)dstages, nst, (uint32_t)items, (uint32_t *)state, spin_limit, diag_device());
     rc = check_launch("keyswitch_batch");
@@ -398,4 +405,11 @@ extern "C" int heal_keyswitch_batch(const heal_keyswitch_job *jobs, int64_t coun
                                                             " writes memory job " + std::to_string(j) + " uses");
     }
   return ks_chunk(jobs, count, 0);
+}
+
+extern "C" int heal_keyswitch_batch_test_wait(uint32_t spin_limit, int stall) {
+  if (spin_limit == 0) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_keyswitch_batch_test_wait: spin_limit must be positive");
+  g_ks_spin_limit = spin_limit;
+  g_ks_stall = stall != 0;
+  return HEAL_OK;
 }

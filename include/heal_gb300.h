@@ -77,7 +77,9 @@ const char *heal_last_error(void);
 
 /* Waits for all enqueued work, then prints (to stderr) the diagnostics
  * kernels recorded since the last synchronisation, e.g. the
- * g_decomposition capacity warnings (g_decomposition_impl.cpp:58-65). */
+ * g_decomposition capacity warnings (g_decomposition_impl.cpp:58-65), and
+ * returns HEAL_ERR_RUNTIME if a heal_keyswitch_batch dependency wait ran out
+ * since then (the report is consumed: the next call returns HEAL_OK). */
 int heal_synchronize(void);
 
 /* The stream every compute call is enqueued on (a cudaStream_t). */
@@ -126,7 +128,8 @@ int heal_free(void *ptr);
 /* Host -> device copy of `bytes` (pageable or pinned host memory).
  * Enqueued on the library stream; returns when the source may be reused. */
 int heal_h2d(void *dst_device, const void *src_host, size_t bytes);
-/* Device -> host copy; waits for all earlier work on the stream first. */
+/* Device -> host copy; waits for all earlier work on the stream first and
+ * reports its diagnostics as heal_synchronize does. */
 int heal_d2h(void *dst_host, const void *src_device, size_t bytes);
 /* Asynchronous variants for pinned host memory (no wait). */
 int heal_h2d_async(void *dst_device, const void *src_host, size_t bytes);
@@ -329,6 +332,14 @@ typedef struct heal_keyswitch_job {
   heal_tensor result;
 } heal_keyswitch_job;
 int heal_keyswitch_batch(const heal_keyswitch_job *jobs, int64_t count);
+
+/* Test hook of heal_keyswitch_batch's failure path (no counterpart in
+ * HEAL): later batches give up a dependency wait after spin_limit polls of
+ * 256 ns (default 2^22, about a second), and with stall != 0 every job's
+ * tail waits for one tile more than its previous stage has, so those waits
+ * run out and the next heal_synchronize returns HEAL_ERR_RUNTIME.  Call it
+ * again with stall = 0 (and the default limit) to restore normal runs. */
+int heal_keyswitch_batch_test_wait(uint32_t spin_limit, int stall);
 
 /* The head of a keyswitch's digit transform in one call (an extension: HEAL
  * has no such op).  Defined as the composition of HEAL's own calls

@@ -86,3 +86,26 @@ def test_batch_argument_errors_write_nothing():
     for o in rk.outs:
         assert not o.numpy().any()
     capi.keyswitch_batch([])  # nothing to do
+
+
+def test_wait_that_runs_out_is_reported_and_the_context_stays_usable():
+    """Failure path: with the test hook every tail waits for a tile that never
+    comes; the waits give up after their limit (here 2^15 polls, ~10 ms), the
+    kernel ends, heal_synchronize reports the timeout, and the next batch
+    runs normally on the same context."""
+    rk = RaggedKeyswitch(count=3, logns=(12,), lmin=2, lmax=3, seed=11)
+    want = per_call(rk)
+    lib = capi.lib()
+    capi.check(lib.heal_keyswitch_batch_test_wait(1 << 15, 1))
+    try:
+        clear(rk)
+        rk.run_batched()
+        with pytest.raises(RuntimeError, match="ran out"):
+            capi.synchronize()
+    finally:
+        capi.check(lib.heal_keyswitch_batch_test_wait(1 << 22, 0))
+    capi.synchronize()  # the report was consumed
+    clear(rk)
+    rk.run_batched()
+    for i, w in enumerate(want):
+        assert np.array_equal(rk.outs[i].numpy(), w), i
