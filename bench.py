@@ -1090,6 +1090,94 @@ def ntt_probe(args):
     return 0
 
 
+def strided_probe(args):
+    """--mode strided: the strided and batched kernels, each call timed with
+    CUDA events (for ncu captures): heal_copy_strided of a transposed
+    [65536, 64] int64 view (make_contiguous's gather), heal_modmul_ttt of a
+    [64, 65536] product whose second operand is broadcast over the rows (the
+    vector-unit strided kernel), heal_permute of a [8, 4096, 64] source read
+    through a transposed view (the general gather), and heal_ntt_batch of 64
+    ragged transforms (N 2^12..2^16, 2..8 limbs, 50-bit primes)."""
+    import torch
+    import heal_gb300
+    from heal_gb300 import capi
+    from heal_gb300 import params as P
+    heal_gb300.build()
+    capi.check(capi.lib().heal_init(0))
+    stream = torch.cuda.ExternalStream(capi.stream())
+    rng = np.random.default_rng(5)
+    qs = np.array(P.ntt_primes(1 << 50, 1 << 12, 64), np.int64)
+    # copy_strided: the transpose of a [64, 65536] tensor viewed [65536, 64]
+    src = capi.DeviceArray.from_numpy(P.residues(1, (64, 1 << 16), np.resize(qs, 1 << 16)))
+    srcT = capi.DeviceArray(src.buf, np.int64, (1 << 16, 64), (1, 1 << 16), src.offset)
+    dst = capi.DeviceArray.empty((1 << 16, 64), np.int64)
+    # modmul with b broadcast over the rows: result [64, 65536] contiguous, b [1, 65536] (stride 0 on rows)
+    a = capi.DeviceArray.from_numpy(P.residues(2, (64, 1 << 16), np.resize(qs, 1 << 16)))
+    b = capi.DeviceArray.from_numpy(P.residues(3, (1, 1 << 16), np.resize(qs, 1 << 16)))
+    pv = capi.DeviceArray.from_numpy(np.resize(qs, 1 << 16))
+    prod = capi.DeviceArray.empty((64, 1 << 16), np.int64)
+    # permute of a source read through a transposed view: [8, 4096, 64] from a [64, 4096, 8] buffer
+    pbuf = capi.DeviceArray.from_numpy(rng.integers(0, 1 << 40, size=(64, 4096, 8), dtype=np.int64))
+    psrc = capi.DeviceArray(pbuf.buf, np.int64, (8, 4096, 64), (1, 8, 4096 * 8), pbuf.offset)
+    perms = capi.DeviceArray.from_numpy(np.stack([rng.permutation(4096) for _ in range(8)]).astype(np.int64))
+    pout = capi.DeviceArray.empty((8, 4096, 64), np.int64)
+    # a ragged batch of forward transforms
+    jobs, keep = [], []
+    for i in range(64):
+        n, l = 1 << int(12 + i % 5), 2 + i % 7
+        q = P.ntt_primes(1 << 50, n, l)
+        pp, perm, tw, _, _ = P.ntt_tables(q, n)
+        arrs = [capi.DeviceArray.from_numpy(v) for v in (P.residues(100 + i, (2, n, 1, l), q), pp, perm, tw)]
+        out = capi.DeviceArray.empty((2, n, 1, l), np.int64)
+        keep += arrs + [out]
+        jobs.append((arrs[0], arrs[1], arrs[2], arrs[3], None, out))
+    calls = {"copy_strided": lambda: capi.call("heal_copy_strided", srcT, dst),
+             "modmul_broadcast": lambda: capi.call("heal_modmul_ttt", a, b, pv, prod),
+             "permute_general": lambda: capi.call("heal_permute", psrc, perms, pout, 0, 1),
+             "ntt_batch_64": lambda: capi.ntt_batch(False, jobs)}
+    res = {}
+    for name, fn in calls.items():
+        for _ in range(args.warmup):
+            fn()
+        capi.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        res[name] = e0.elapsed_time(e1) / args.steps
+    print(json.dumps({"mode": "strided", "ms_per_call": res}), flush=True)
+    return 0
+
+
+def keyswitch_batch_probe(args):
+    """--mode ksbatch: one heal_keyswitch_batch of --batch ciphertexts (ring
+    degrees 2^12..2^16, 2..8 limbs), timed with CUDA events (for ncu)."""
+    import torch
+    import heal_gb300
+    from heal_gb300 import capi
+    from heal_gb300.configs import RaggedKeyswitch
+    heal_gb300.build()
+    capi.check(capi.lib().heal_init(0))
+    stream = torch.cuda.ExternalStream(capi.stream())
+    rk = RaggedKeyswitch(count=args.batch, lmin=2, lmax=8, seed=31)
+    for _ in range(args.warmup):
+        rk.run_batched()
+    capi.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        rk.run_batched()
+    e1.record(stream)
+    e1.synchronize()
+    capi.synchronize()
+    print(json.dumps({"mode": "ksbatch", "ciphertexts": args.batch, "ms_per_call": e0.elapsed_time(e1) / args.steps,
+                      "algorithmic_GBps": rk.bytes_per_step() / (e0.elapsed_time(e1) / args.steps / 1e3) / 1e9}),
+          flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1102,7 +1190,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default NTT plans instead of autotuned ones")
     ap.add_argument("--configs", default=",".join(WORKLOADS),
                     help="comma-separated configurations reported beside the headline")
-    ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request", "tail"])
+    ap.add_argument("--mode", default="chain", choices=["chain", "ntt", "request", "tail", "strided", "ksbatch"])
     ap.add_argument("--d", type=int, default=64, help="--mode request: matrix dimension")
     ap.add_argument("--n", type=int, default=1 << 14, help="--mode request: ring degree")
     ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
@@ -1119,6 +1207,10 @@ def main():
         return ntt_probe(args)
     if args.mode == "tail":
         return tail_probe(args)
+    if args.mode == "strided":
+        return strided_probe(args)
+    if args.mode == "ksbatch":
+        return keyswitch_batch_probe(args)
     if args.mode == "request":
         return request_probe(args)
     if args.impl == "reference":
