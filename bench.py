@@ -911,6 +911,7 @@ def serving_config(args, count: int = 4000, rate: float = 2000.0):
                     break
             out["fused_rate_sweep"] = sweep
             out["fused_capacity_req_per_s"] = max(x["throughput_req_per_s"] for x in sweep + [out[name]])
+            out["fused_from_transcripts"] = serve_transcripts(srv)
             out["cpu_baseline"] = serving_cpu(srv)
             out["roofline"] = dict(hbm_roofline(out[name]["algorithmic_GBps"] * 1e9, 1e3,
                                                 "the fused serving loop at the offered rate"),
@@ -918,6 +919,33 @@ def serving_config(args, count: int = 4000, rate: float = 2000.0):
                                         "the loop is bound by the offered load, not by HBM")
         del srv
     return out
+
+
+def serve_transcripts(srv, count: int = 240, rate: float = 500.0):
+    """The fused path with every request arriving as a HEAL transcript (JSON,
+    base64 diagonals), decoded on arrival inside the loop: latency and
+    throughput with the intake included, and the decode time alone."""
+    import torch
+    from heal_gb300 import serving as S
+    reqs = S.poisson_schedule(count, rate, 808, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
+    texts = {r.rid: S.matvec_transcript(S.ct_name(r.n, r.l, r.ct), srv.host_mats[(r.d, r.l, r.mat)][r.n])
+             for r in reqs}
+    dec = []
+    for r in reqs[:24]:
+        t1 = time.perf_counter()
+        srv.from_transcript(texts[r.rid], r.rid, 0.0)
+        dec.append((time.perf_counter() - t1) * 1e3)
+    sample = [r.rid for r in reqs[:: count // 8]]
+    st = srv.run(reqs, keep=sample, transcripts=texts)
+    torch.cuda.synchronize()
+    same = all(np.array_equal(srv.out_host[i], srv.alone(reqs[i])) for i in sample)
+    ms = lambda xs, q: S.percentile(xs, q) * 1e3
+    return {"requests": count, "offered_req_per_s": count / reqs[-1].arrival,
+            "throughput_req_per_s": count / st.span, "p50_ms": ms(st.latencies, 50), "p99_ms": ms(st.latencies, 99),
+            "decode_ms_p50": statistics.median(dec), "decode_ms_max": max(dec),
+            "mean_transcript_MB": sum(len(t) for t in texts.values()) / count / 1e6, "alone_equals_mix": same,
+            "intake": "HEAL's JSON transcript format: host_to_device of the diagonals, matvec on a resident "
+                      "ciphertext, device_to_host; decoded on arrival inside the timed loop"}
 
 
 def serving_server(fused):

@@ -20,6 +20,16 @@ same in one heal_modmul_axis_sum over S = [d, N/d, d, 2, L] (slot j = u*d + s):
 the ciphertext and the d x d diagonals enter as stride-only views and the
 rotation gathers over the flattened slot pair, so no stack is written.
 
+Intake.  A request can arrive as a transcript in HEAL's wire format (JSON
+with base64 tensors, python_execution/lattica_heal_runtime/serialization.py:
+15-148, read as runtime.py:79-93 reads it): a host_to_device of the d x d
+matrix's diagonals, a `matvec` device op on a resident ciphertext the server
+names ("ct/N/L/c") and on the uploaded diagonals, and a device_to_host of the
+result.  matvec_transcript writes one (the client side);
+MatVecServer.from_transcript decodes and checks it and returns the Request
+that the loop admits like any other, the decoded diagonals taking the place
+of the server's own matrix.
+
 Scheduling.  Arrivals follow a seeded Poisson process.  A request is
 admitted, in arrival order, once its device footprint (rotated stack,
 diagonals, output) fits in a fixed HBM arena; the arena's host-side
@@ -95,6 +105,7 @@ class Request:
     done: float = -1.0
 
     fused: bool = False
+    host_diag: object = None  # decoded from the request's transcript (else the server's own matrix)
 
     def footprint(self) -> int:
         """Device bytes the request holds while in flight: the rotated stack
@@ -113,6 +124,52 @@ def diag_bytes(l, d):
 
 def out_bytes(n, l):
     return 2 * n * l * 8
+
+
+def ct_name(n: int, l: int, c: int) -> str:
+    """The name a transcript uses for resident ciphertext c of shape [2, n, l]."""
+    return f"ct/{n}/{l}/{c}"
+
+
+def matvec_transcript(ct: str, diagonals) -> str:
+    """A request as a HEAL transcript (JSON): upload the diagonals
+    [d, 1, 1, d, L] (int64 torch tensor), `matvec` of resident ciphertext
+    `ct` by them, download of the result [2, N, L].  The download's expected
+    tensor is an empty placeholder: the client has no result to verify."""
+    import torch
+    from .runtime import DeviceTensorPointer, TranscriptBuilder, dumps
+    tb = TranscriptBuilder(prefix="r")
+    tb.segment("matvec")
+    dg = tb.host_to_device(diagonals)
+    out = tb.op("matvec", DeviceTensorPointer(ct, torch.int64), dg, int(diagonals.shape[0]), dtype=torch.int64)
+    tb.device_to_host(out, torch.zeros(0, dtype=torch.int64))
+    tb.free(dg, out)
+    tb.end_segment()
+    return dumps(tb.transcript())
+
+
+def parse_matvec_transcript(transcript):
+    """(ciphertext name, d, diagonals) of a matvec request transcript; raises
+    ValueError for any other shape of transcript."""
+    from .runtime import DeviceOpArgType as A
+    from .runtime import ExecutionTranscriptOpType as K
+    ops = [(k, v) for k, v in transcript.transcript if k in (K.DEVICE_OP, K.FREE_DEVICE_TENSOR)]
+    names = [v.name for k, v in ops if k == K.DEVICE_OP]
+    if names != ["host_to_device", "matvec", "device_to_host"]:
+        raise ValueError(f"not a matvec request: device ops {names}")
+    h2d, mv, d2h = [v for k, v in ops if k == K.DEVICE_OP]
+    up = h2d.out.value.inf_name
+    a0, a1, a2 = (mv.args + [None, None, None])[:3]
+    if not (len(mv.args) == 3 and a0.arg_type == A.DEVICE_TENSOR and a1.arg_type == A.DEVICE_TENSOR and
+            a1.value.inf_name == up and a2.arg_type == A.INT):
+        raise ValueError("matvec takes (resident ciphertext, the uploaded diagonals, d)")
+    if d2h.args[0].value.inf_name != mv.out.value.inf_name:
+        raise ValueError("the request must download the matvec result")
+    diag = h2d.args[0].value.tensor
+    d = int(a2.value)
+    if diag.ndim != 5 or diag.shape[0] != d or diag.shape[3] != d or diag.shape[1] != 1 or diag.shape[2] != 1:
+        raise ValueError(f"diagonals must have shape [d, 1, 1, d, L], got {tuple(diag.shape)}")
+    return a0.value.inf_name, d, diag
 
 
 def poisson_schedule(count: int, rate: float, seed: int, ns, ds, lmin: int, lmax: int, cts: int, mats: int):
@@ -140,7 +197,7 @@ class LoopStats:
 
 
 def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max_inflight: int = 64,
-          timeout: float | None = None):
+          timeout: float | None = None, intake=None):
     """Runs the admission loop.  issue(req, offset) enqueues the request's GPU
     work and returns an object with query() -> bool (True once finished) and
     finish() (called once, after query() turned True).  Requests are admitted
@@ -148,13 +205,17 @@ def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max
     than the whole arena raises MemoryError; with `timeout` (seconds), a
     request still unfinished that long after its admission raises
     TimeoutError, so a device that stopped answering ends the loop instead
-    of leaving it polling."""
+    of leaving it polling.  With `intake`, each request is replaced on
+    arrival by intake(request) (a transcript decoded into the request it
+    describes); the time it takes counts toward the request's latency."""
     pending = sorted(requests, key=lambda r: r.arrival)
     queue, inflight, st = [], [], LoopStats()
     nxt, t0 = 0, clock()
     while nxt < len(pending) or queue or inflight:
         now = clock() - t0
         while nxt < len(pending) and pending[nxt].arrival <= now:
+            if intake is not None:
+                pending[nxt] = intake(pending[nxt])
             queue.append(pending[nxt])
             nxt += 1
         st.max_queue = max(st.max_queue, len(queue))
@@ -234,6 +295,7 @@ class MatVecServer:
         self.rr = 0
         self.out_host = {}
         self.keep = set()                    # request ids whose output is kept
+        self.pinned = {}                     # shape -> free pinned buffers for decoded diagonals
 
     # views into the arena
     def _view(self, off, shape):
@@ -274,7 +336,7 @@ class MatVecServer:
         try:
             o_diag = off if self.fused else off + stack_bytes(n, l, d)
             out = self._view(o_diag + diag_bytes(l, d), (2, n, l))
-            host = self.host_mats[(d, l, req.mat)][n]
+            host = req.host_diag if req.host_diag is not None else self.host_mats[(d, l, req.mat)][n]
             capi.check(capi.lib().heal_h2d_async(ctypes.c_void_p(self.arena_buf.ptr.value + o_diag),
                                                  ctypes.c_void_p(host.data_ptr()), diag_bytes(l, d)))
             for fn in self.calls(req, off).values():
@@ -301,6 +363,8 @@ class MatVecServer:
             def finish(self):
                 if req.rid in server.keep:
                     server.out_host[req.rid] = res.numpy().copy()
+                if req.host_diag is not None:  # its upload has completed: the buffer can serve another request
+                    server.pinned.setdefault(tuple(req.host_diag.shape), []).append(req.host_diag)
         return Handle()
 
     def split_ms(self, req: Request, reps: int = 5) -> dict:
@@ -328,6 +392,27 @@ class MatVecServer:
             self.capi.check(self.capi.lib().heal_set_stream(None))
             self.arena.free(off)
 
+    def from_transcript(self, text: str, rid: int, arrival: float) -> Request:
+        """Decodes a matvec request transcript (JSON) into a Request on a
+        resident ciphertext; the diagonals are copied into a pinned buffer
+        (from a pool; it returns there when the request completes) for the
+        request's asynchronous upload."""
+        from .runtime import loads
+        name, d, diag = parse_matvec_transcript(loads(text))
+        try:
+            tag, n, l, c = name.split("/")
+            n, l, c = int(n), int(l), int(c)
+            assert tag == "ct" and (n, l) in self.ct and 0 <= c < len(self.ct[(n, l)])
+        except (ValueError, AssertionError):
+            raise ValueError(f"no resident ciphertext named {name!r}") from None
+        if d not in self.ds or n % d or tuple(diag.shape) != (d, 1, 1, d, l):
+            raise ValueError(f"request of d = {d} on {name} does not fit the server")
+        src = self.torch.as_tensor(diag, dtype=self.torch.int64)
+        pool = self.pinned.setdefault(tuple(src.shape), [])
+        host = pool.pop() if pool else self.torch.empty(tuple(src.shape), dtype=self.torch.int64, pin_memory=True)
+        host.copy_(src)
+        return Request(rid, arrival, n, l, d, c, -1, host_diag=host)
+
     def alone(self, req: Request) -> np.ndarray:
         """The request run by itself (one stream, nothing else in flight)."""
         req.fused = self.fused
@@ -351,15 +436,24 @@ class MatVecServer:
                     self.alone(Request(rid, 0.0, n, l, d, 0, 0))
         self.torch.cuda.synchronize()
 
-    def run(self, requests, keep=(), timeout: float | None = 60.0):
+    def run(self, requests, keep=(), timeout: float | None = 60.0, transcripts=None):
         """Serves `requests`; a request still unfinished `timeout` seconds
         after its admission (admitted requests take milliseconds) raises
-        TimeoutError."""
+        TimeoutError.  With `transcripts` ({rid: JSON text}), a request whose
+        rid has one arrives as that transcript and is decoded on arrival."""
         for r in requests:
             r.fused = self.fused
         self.keep = set(keep)
         self.out_host = {}
-        return serve(requests, self.arena, self.issue, timeout=timeout)
+        intake = None
+        if transcripts:
+            def intake(r):
+                if r.rid not in transcripts:
+                    return r
+                q = self.from_transcript(transcripts[r.rid], r.rid, r.arrival)
+                q.fused = self.fused
+                return q
+        return serve(requests, self.arena, self.issue, timeout=timeout, intake=intake)
 
     @staticmethod
     def bytes_moved(req: Request) -> int:

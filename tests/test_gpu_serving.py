@@ -36,3 +36,24 @@ def test_serving_outputs_match_oracle_and_standalone(fused):
         got = srv.out_host[r.rid]
         assert np.array_equal(got, oracle_product(srv, r)), r
         assert np.array_equal(got, srv.alone(r)), r
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_requests_arriving_as_transcripts(fused):
+    """A burst whose requests arrive as HEAL transcripts (decoded on arrival)
+    gives, request by request, what the same requests give issued directly
+    and what the oracle gives."""
+    srv = S.MatVecServer(ns=(256, 512), ds=(2, 4, 8), lmin=2, lmax=4, bits=40, cts=2, mats=2,
+                         budget=1 << 20, streams=3, seed=23, fused=fused)
+    srv.warm()
+    reqs = S.poisson_schedule(40, 50000.0, 12, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
+    texts = {r.rid: S.matvec_transcript(S.ct_name(r.n, r.l, r.ct), srv.host_mats[(r.d, r.l, r.mat)][r.n])
+             for r in reqs if r.rid % 2 == 0}
+    direct = {r.rid: srv.alone(S.Request(r.rid, 0.0, r.n, r.l, r.d, r.ct, r.mat)) for r in reqs}
+    st = srv.run(reqs, keep=[r.rid for r in reqs], transcripts=texts)
+    assert len(st.latencies) == len(reqs)
+    for r in reqs:
+        assert np.array_equal(srv.out_host[r.rid], direct[r.rid]), r
+        assert np.array_equal(srv.out_host[r.rid], oracle_product(srv, r)), r
+    with pytest.raises(ValueError, match="resident"):
+        srv.from_transcript(S.matvec_transcript("ct/999/2/0", srv.host_mats[(2, 2, 0)][256]), 0, 0.0)

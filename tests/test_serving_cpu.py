@@ -126,3 +126,44 @@ def test_unfinished_request_times_out():
     st = S.serve(S.poisson_schedule(5, 1000.0, 3, (256,), (2,), 2, 2, 1, 1), S.Arena(1 << 30),
                  lambda r, o: Handle(S.Request(0, 0.0, 256, 2, 2, 0, 0)), clock=FakeClock(), timeout=0.01)
     assert len(st.latencies) == 5
+
+
+def test_matvec_request_transcript_round_trips_through_heal_json():
+    """A request written as a HEAL transcript (JSON, base64 tensors) decodes
+    back to its ciphertext name, d and diagonals; other transcripts are
+    refused."""
+    import torch
+    from heal_gb300.runtime import TranscriptBuilder, dumps, loads
+    diag = torch.arange(4 * 4 * 3, dtype=torch.int64).reshape(4, 1, 1, 4, 3)
+    text = S.matvec_transcript(S.ct_name(256, 3, 1), diag)
+    name, d, got = S.parse_matvec_transcript(loads(text))
+    assert (name, d) == ("ct/256/3/1", 4) and torch.equal(torch.as_tensor(got), diag)
+    # a transcript with another op, or diagonals of the wrong shape
+    tb = TranscriptBuilder()
+    x = tb.host_to_device(diag)
+    tb.op("axis_modsum", x, 0, dtype=torch.int64)
+    with pytest.raises(ValueError, match="not a matvec request"):
+        S.parse_matvec_transcript(loads(dumps(tb.transcript())))
+    with pytest.raises(ValueError, match="shape"):
+        S.parse_matvec_transcript(loads(S.matvec_transcript("ct/256/3/1", diag.reshape(4, 1, 4, 1, 3))))
+
+
+def test_intake_decodes_each_request_on_arrival():
+    """serve(..., intake=) replaces each request by intake(request) when it
+    arrives, before admission."""
+    seen = []
+
+    def intake(r):
+        seen.append(r.rid)
+        return S.Request(r.rid, r.arrival, r.n, r.l, r.d, r.ct, r.mat)
+
+    class Done:
+        def query(self):
+            return True
+
+        def finish(self):
+            pass
+
+    reqs = [S.Request(i, 0.0, 256, 2, 4, 0, 0) for i in range(5)]
+    st = S.serve(reqs, S.Arena(1 << 20), lambda r, off: Done(), intake=intake)
+    assert seen == list(range(5)) and len(st.latencies) == 5
