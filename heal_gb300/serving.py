@@ -133,9 +133,11 @@ def ct_name(n: int, l: int, c: int) -> str:
 
 def matvec_transcript(ct: str, diagonals) -> str:
     """A request as a HEAL transcript (JSON): upload the diagonals
-    [d, 1, 1, d, L] (int64 torch tensor), `matvec` of resident ciphertext
-    `ct` by them, download of the result [2, N, L].  The download's expected
-    tensor is an empty placeholder: the client has no result to verify."""
+    [d, 1, 1, d, L] (int64; a numpy array travels as np.save bytes, a torch
+    tensor as torch.save bytes, both base64, as HEAL encodes them),
+    `matvec` of resident ciphertext `ct` by them, download of the result
+    [2, N, L].  The download's expected tensor is an empty placeholder: the
+    client has no result to verify."""
     import torch
     from .runtime import DeviceTensorPointer, TranscriptBuilder, dumps
     tb = TranscriptBuilder(prefix="r")
@@ -363,9 +365,15 @@ class MatVecServer:
             def finish(self):
                 if req.rid in server.keep:
                     server.out_host[req.rid] = res.numpy().copy()
-                if req.host_diag is not None:  # its upload has completed: the buffer can serve another request
-                    server.pinned.setdefault(tuple(req.host_diag.shape), []).append(req.host_diag)
+                server.recycle(req)  # its upload has completed
         return Handle()
+
+    def recycle(self, req: Request):
+        """Returns a decoded request's pinned diagonals buffer to the pool
+        (once nothing reads it any more)."""
+        if req.host_diag is not None:
+            self.pinned.setdefault(tuple(req.host_diag.shape), []).append(req.host_diag)
+            req.host_diag = None
 
     def split_ms(self, req: Request, reps: int = 5) -> dict:
         """Median CUDA-event time of each HEAL call of the request (its
@@ -392,11 +400,13 @@ class MatVecServer:
             self.capi.check(self.capi.lib().heal_set_stream(None))
             self.arena.free(off)
 
-    def from_transcript(self, text: str, rid: int, arrival: float) -> Request:
-        """Decodes a matvec request transcript (JSON) into a Request on a
-        resident ciphertext; the diagonals are copied into a pinned buffer
-        (from a pool; it returns there when the request completes) for the
-        request's asynchronous upload."""
+    def from_transcript(self, text, rid: int, arrival: float) -> Request:
+        """Decodes a matvec request transcript (JSON text, or its UTF-8 bytes
+        as they arrive) into a Request on a resident ciphertext; the
+        diagonals are copied into a pinned buffer (from a pool; it returns
+        there when the request completes) for the request's asynchronous
+        upload.  The payload is decoded by the C library's base64 decoder
+        and, for a numpy payload, used in place (runtime.serialization)."""
         from .runtime import loads
         name, d, diag = parse_matvec_transcript(loads(text))
         try:

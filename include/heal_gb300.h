@@ -141,6 +141,19 @@ int heal_host_free(void *ptr);
  * this library, so tables derived from it are rebuilt on their next use. */
 int heal_mark_modified(void *ptr);
 
+/* Host-side decoding of a transcript's tensor payload: `len` bytes of
+ * base64 text at `src` (RFC 4648 standard alphabet, '=' padding) into `dst`
+ * (capacity `cap` bytes), split over up to `threads` host threads (<= 0: one
+ * per core, at most 16; runs of 256 KB of text at least); *written = the
+ * decoded length.  Replaces the base64.b64decode of HEAL's decode_tensor
+ * (python_execution/lattica_heal_runtime/serialization.py:31) on the request
+ * path of a server that takes transcripts.  Only the canonical encoding is
+ * accepted (length a multiple of 4, padding only at the end, no other
+ * characters): anything else, or a `dst` too small, returns
+ * HEAL_ERR_INVALID_ARGUMENT, and the caller decodes such text leniently.
+ * Touches no GPU. */
+int heal_base64_decode(const char *src, size_t len, void *dst, size_t cap, size_t *written, int threads);
+
 /* Strided gather of `src` into `dst` (same dims, any strides, any dtype):
  * the copy inside make_contiguous (include/contiguous.h:19-20;
  * example_impl/contiguous_impl.cpp:9-52). */

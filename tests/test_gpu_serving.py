@@ -57,3 +57,26 @@ def test_requests_arriving_as_transcripts(fused):
         assert np.array_equal(srv.out_host[r.rid], oracle_product(srv, r)), r
     with pytest.raises(ValueError, match="resident"):
         srv.from_transcript(S.matvec_transcript("ct/999/2/0", srv.host_mats[(2, 2, 0)][256]), 0, 0.0)
+
+
+def test_large_transcripts_decoded_natively():
+    """Requests whose diagonals (up to 64 x 64 x 6 int64, 256 KB of base64)
+    are cut out of the JSON and decoded by heal_base64_decode, as np.save
+    payloads used in place and as torch.save payloads, arriving as bytes:
+    every result equals the request issued directly and the oracle."""
+    srv = S.MatVecServer(ns=(4096,), ds=(16, 64), lmin=4, lmax=6, bits=40, cts=2, mats=2,
+                         budget=1 << 26, streams=3, seed=29, fused=True)
+    srv.warm()
+    reqs = S.poisson_schedule(24, 20000.0, 31, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
+    assert {r.d for r in reqs} == {16, 64}
+    texts = {}
+    for r in reqs:
+        diag = srv.host_mats[(r.d, r.l, r.mat)][r.n]
+        texts[r.rid] = S.matvec_transcript(S.ct_name(r.n, r.l, r.ct), diag.numpy() if r.rid % 2 else diag).encode()
+    direct = {r.rid: srv.alone(S.Request(r.rid, 0.0, r.n, r.l, r.d, r.ct, r.mat)) for r in reqs}
+    st = srv.run(reqs, keep=[r.rid for r in reqs], transcripts=texts)
+    assert len(st.latencies) == len(reqs)
+    for r in reqs:
+        assert np.array_equal(srv.out_host[r.rid], direct[r.rid]), r
+    for r in reqs[:4]:
+        assert np.array_equal(srv.out_host[r.rid], oracle_product(srv, r)), r
