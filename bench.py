@@ -300,13 +300,19 @@ def our_arm(args):
         if world > 1:
             torch.distributed.barrier()
 
+    # host time of the last timed loop's enqueueing (perf_counter around the
+    # loop): when it approaches the device time, the host bounds the rate
+    host_ms = {"last": 0.0}
+
     def timed(fn, steps):
         barrier()
         start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = capi.launches()
         start.record(stream)
+        h0 = time.perf_counter()
         for s in range(steps):
             fn(s)
+        host_ms["last"] = (time.perf_counter() - h0) * 1e3
         stop.record(stream)
         stop.synchronize()
         barrier()
@@ -350,8 +356,10 @@ def our_arm(args):
         start.record(stream)
         for sd in sides:
             sd.wait_event(start)
+        h0 = time.perf_counter()
         for s in range(steps):
             fn(s)
+        host_ms["last"] = (time.perf_counter() - h0) * 1e3
         for sd in sides:
             joined = torch.cuda.Event()
             joined.record(sd)
@@ -369,6 +377,7 @@ def our_arm(args):
     with Clocks(local) as clk:
         ms, launches = timed2(chain_step2, nch)
     clocks = clk.summary()
+    host_us = {"resident": host_ms["last"] * 1e3 / nch}
     value = whole_job_rate(nch, world, ms)
     for w in range(args.warmup):
         chain_step(w)
@@ -468,33 +477,38 @@ def our_arm(args):
 
     # ---- end to end through the C ABI from pinned host memory.  Every step
     # copies its ciphertext in (H2D) and its result out (D2H) inside the timed
-    # region; the copies run on their own streams, double-buffered, so the
-    # H2D of step s+1 and the D2H of step s-1 overlap the chain of step s.
+    # region.  The copies run on their own streams into a ring of E2E_RING
+    # device buffers per direction, so the H2D of the next steps runs ahead
+    # while the two chains in flight compute, and the D2H of a finished chain
+    # overlaps the chains after it (with two buffers, a chain's input copy
+    # could only start once the chain two steps back had finished, and one
+    # copy time per pair of chains ran with a single chain in flight).
+    E2E_RING = 4
     nbytes = 2 * N * L * 8
     import ctypes
     lib = capi.lib()
     pin_in = ctypes.c_void_p()
     capi.check(lib.heal_host_alloc(nbytes, ctypes.byref(pin_in)))
-    pin_out = [ctypes.c_void_p() for _ in range(2)]
+    pin_out = [ctypes.c_void_p() for _ in range(E2E_RING)]
     for p_ in pin_out:
         capi.check(lib.heal_host_alloc(nbytes, ctypes.byref(p_)))
     ctypes.memmove(pin_in, cts_host[0].ctypes.data, nbytes)
-    dev_in = [capi.DeviceArray.empty(ch.shape(), np.int64, zero=False) for _ in range(2)]
-    dev_out = [capi.DeviceArray.empty(ch.shape(), np.int64, zero=False) for _ in range(2)]
+    dev_in = [capi.DeviceArray.empty(ch.shape(), np.int64, zero=False) for _ in range(E2E_RING)]
+    dev_out = [capi.DeviceArray.empty(ch.shape(), np.int64, zero=False) for _ in range(E2E_RING)]
     s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
-    ev_in, ev_comp, ev_out = ([torch.cuda.Event() for _ in range(2)] for _ in range(3))
+    ev_in, ev_comp, ev_out = ([torch.cuda.Event() for _ in range(E2E_RING)] for _ in range(3))
     use = lambda st: capi.check(lib.heal_set_stream(st.cuda_stream if st is not None else None))
 
     def e2e_step(s):
-        b = s % 2
+        b = s % E2E_RING
         s_in.wait_event(ev_comp[b])                       # the chain that last read dev_in[b]
         use(s_in)
         capi.check(lib.heal_h2d_async(ctypes.c_void_p(dev_in[b].ptr), pin_in, nbytes))
         ev_in[b].record(s_in)
-        cs, chb = (stream, ch) if b == 0 else (side, ch2)  # two chains in flight, as in the resident run
+        cs, chb = (stream, ch) if s % 2 == 0 else (side, ch2)  # two chains in flight, as in the resident run
         cs.wait_event(ev_in[b])
         cs.wait_event(ev_out[b])                          # the copy that last read dev_out[b]
-        use(None if b == 0 else side)
+        use(None if cs is stream else side)
         chb.run(dev_in[b], dev_out[b])
         ev_comp[b].record(cs)
         s_out.wait_event(ev_comp[b])
@@ -509,10 +523,12 @@ def our_arm(args):
         start.record(stream)
         s_in.wait_event(start)
         side.wait_event(start)
+        h0 = time.perf_counter()
         for s in range(steps):
             e2e_step(s)
-        stream.wait_event(ev_out[(steps - 1) % 2])
-        stream.wait_event(ev_out[steps % 2])
+        host_ms["last"] = (time.perf_counter() - h0) * 1e3
+        for ev in ev_out:
+            stream.wait_event(ev)
         stop.record(stream)
         stop.synchronize()
         barrier()
@@ -522,6 +538,7 @@ def our_arm(args):
         e2e_step(w)
     e2e_ms = e2e_timed(nch)
     e2e = whole_job_rate(nch, world, e2e_ms)
+    host_us["e2e"] = host_ms["last"] * 1e3 / nch
     torch.cuda.synchronize()
     want = outs[0].numpy()
     for p_ in pin_out:
@@ -571,9 +588,11 @@ def our_arm(args):
                 "int_roofline": int_roofline,
                 "e2e": {"value": e2e, "unit": "chains/s", "h2d_bytes_per_step": nbytes * CHAINS_PER_STEP,
                         "d2h_bytes_per_step": nbytes * CHAINS_PER_STEP,
-                        "pipeline": "H2D and D2H on their own streams, consecutive chains alternating between two "
-                                    "compute streams",
+                        "pipeline": f"H2D and D2H on their own streams into a ring of {E2E_RING} device buffers "
+                                    "per direction, consecutive chains alternating between two compute streams",
                         "serial_value": e2e_serial},
+                "host_us_per_chain": {k: v for k, v in host_us.items()},
+                "device_us_per_chain": {"resident": ms * 1e3 / nch, "e2e": e2e_ms * 1e3 / nch},
                 "gpu_launches": launches, "launches_per_step": launches / args.steps,
                 "split_ms": split_ms, "ntt_plans": plans, "fused_chain": fused_chain,
                 "clocks": clocks, "cpu_baseline": cpu, "configs": configs}
@@ -921,31 +940,40 @@ def serving_config(args, count: int = 4000, rate: float = 2000.0):
     return out
 
 
-def serve_transcripts(srv, count: int = 240, rate: float = 500.0):
-    """The fused path with every request arriving as a HEAL transcript (JSON,
-    base64 diagonals), decoded on arrival inside the loop: latency and
-    throughput with the intake included, and the decode time alone."""
+def serve_transcripts(srv, count: int = 480, runs=((500.0, 0), (2000.0, 0), (2000.0, 4), (4000.0, 4))):
+    """The fused path with every request arriving as a HEAL transcript (the
+    UTF-8 JSON bytes a client sends, the diagonals as base64 np.save
+    payloads), decoded on arrival: latency and throughput with the intake
+    included for each (offered rate, intake threads; 0 = decoded on the
+    loop's own thread), and the decode time alone."""
     import torch
     from heal_gb300 import serving as S
-    reqs = S.poisson_schedule(count, rate, 808, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
-    texts = {r.rid: S.matvec_transcript(S.ct_name(r.n, r.l, r.ct), srv.host_mats[(r.d, r.l, r.mat)][r.n])
-             for r in reqs}
-    dec = []
-    for r in reqs[:24]:
-        t1 = time.perf_counter()
-        srv.from_transcript(texts[r.rid], r.rid, 0.0)
-        dec.append((time.perf_counter() - t1) * 1e3)
-    sample = [r.rid for r in reqs[:: count // 8]]
-    st = srv.run(reqs, keep=sample, transcripts=texts)
-    torch.cuda.synchronize()
-    same = all(np.array_equal(srv.out_host[i], srv.alone(reqs[i])) for i in sample)
-    ms = lambda xs, q: S.percentile(xs, q) * 1e3
-    return {"requests": count, "offered_req_per_s": count / reqs[-1].arrival,
-            "throughput_req_per_s": count / st.span, "p50_ms": ms(st.latencies, 50), "p99_ms": ms(st.latencies, 99),
-            "decode_ms_p50": statistics.median(dec), "decode_ms_max": max(dec),
-            "mean_transcript_MB": sum(len(t) for t in texts.values()) / count / 1e6, "alone_equals_mix": same,
-            "intake": "HEAL's JSON transcript format: host_to_device of the diagonals, matvec on a resident "
-                      "ciphertext, device_to_host; decoded on arrival inside the timed loop"}
+    out = {"intake": "HEAL's JSON transcript format: host_to_device of the diagonals (np.save, base64), matvec on "
+                     "a resident ciphertext, device_to_host; decoded on arrival inside the timed loop (payloads "
+                     "cut out of the JSON and decoded by heal_base64_decode, used in place)", "rates": []}
+    for k, (rate, threads) in enumerate(runs):
+        reqs = S.poisson_schedule(count, rate, 808, srv.ns, srv.ds, srv.lmin, srv.lmax, srv.cts, srv.mats)
+        texts = {r.rid: S.matvec_transcript(S.ct_name(r.n, r.l, r.ct), srv.host_mats[(r.d, r.l, r.mat)][r.n].numpy())
+                 .encode() for r in reqs}
+        if k == 0:
+            dec = {}
+            for r in reqs[:48]:
+                t1 = time.perf_counter()
+                q = srv.from_transcript(texts[r.rid], r.rid, 0.0)
+                dec.setdefault(r.d, []).append((time.perf_counter() - t1) * 1e3)
+                srv.recycle(q)
+            out["decode_ms_p50_by_d"] = {d: statistics.median(v) for d, v in sorted(dec.items())}
+            out["mean_transcript_MB"] = sum(len(t) for t in texts.values()) / count / 1e6
+        sample = [r.rid for r in reqs[:: count // 8]]
+        st = srv.run(reqs, keep=sample, transcripts=texts, intake_threads=threads)
+        torch.cuda.synchronize()
+        same = all(np.array_equal(srv.out_host[i], srv.alone(reqs[i])) for i in sample)
+        ms = lambda xs, q: S.percentile(xs, q) * 1e3
+        out["rates"].append({"intake_threads": threads, "requests": count,
+                             "offered_req_per_s": count / reqs[-1].arrival,
+                             "throughput_req_per_s": count / st.span, "p50_ms": ms(st.latencies, 50),
+                             "p99_ms": ms(st.latencies, 99), "max_queue": st.max_queue, "alone_equals_mix": same})
+    return out
 
 
 def serving_server(fused):

@@ -223,7 +223,16 @@ class DeviceArray:
         return int(np.prod(self.shape)) if self.shape else 1
 
     def desc(self) -> Tensor:
+        """A new descriptor of the view (the caller may edit it)."""
         return desc(self.ptr if self.buf.ptr.value else None, self.dtype, self.shape, self.strides)
+
+    def cdesc(self) -> Tensor:
+        """The view's descriptor, built on first use and shared by every call
+        that only reads it (a view never changes after construction)."""
+        d = self.__dict__.get("_cdesc")
+        if d is None:
+            d = self._cdesc = self.desc()
+        return d
 
     def numpy(self) -> np.ndarray:
         n = self.size
@@ -258,7 +267,7 @@ def _arg(x):
     if x is None:
         return None
     if isinstance(x, DeviceArray):
-        return ctypes.byref(x.desc())
+        return ctypes.byref(x.cdesc())
     return x
 
 

@@ -67,16 +67,20 @@ class _Payload:
         return json.loads(b'"' + self.raw[self.a:self.b] + b'"')
 
 
-def _native_b64decode(p: _Payload):
-    """heal_base64_decode of the payload in place in its text; None when the
-    library is not built or the text is not canonical base64."""
+def _native_b64decode(p: _Payload, sink=None):
+    """heal_base64_decode of the payload in place in its text, into a new
+    array or into sink(nbytes) (a writable uint8 array of at least nbytes);
+    None when the library is not built or the text is not canonical
+    base64."""
     try:
         from .. import capi
         lib = capi.lib()
     except (ImportError, OSError):
         return None
     n = p.b - p.a
-    out = np.empty(n // 4 * 3, np.uint8)
+    out = np.empty(n // 4 * 3, np.uint8) if sink is None else sink(n // 4 * 3)
+    if out.dtype != np.uint8 or out.ndim != 1 or out.size < n // 4 * 3 or not out.flags.writeable:
+        raise ValueError("a payload sink must return a writable 1-D uint8 array of the size asked for")
     written = ctypes.c_size_t(0)
     src = ctypes.cast(ctypes.c_char_p(p.raw), ctypes.c_void_p).value + p.a
     if lib.heal_base64_decode(src, n, out.ctypes.data, out.size, ctypes.byref(written), 0) != 0:
@@ -84,9 +88,9 @@ def _native_b64decode(p: _Payload):
     return memoryview(out)[:written.value]
 
 
-def _b64decode(data):
+def _b64decode(data, sink=None):
     if isinstance(data, _Payload):
-        got = _native_b64decode(data)
+        got = _native_b64decode(data, sink)
         if got is not None:
             return got
         data = data.text()
@@ -117,11 +121,12 @@ def _npy_view(buf: memoryview):
     return np.frombuffer(buf, dtype=dtype, count=count, offset=off).reshape(shape, order="F" if fortran else "C")
 
 
-def decode_tensor(obj: dict):
+def decode_tensor(obj: dict, sink=None):
     """The host tensor of an encoded payload, as HEAL's decode_tensor makes
     it (serialization.py:30-37).  A numpy payload decoded by the C library
-    comes back as an array over the decoded bytes, without np.load's copy."""
-    data = _b64decode(obj["data"])
+    comes back as an array over the decoded bytes, without np.load's copy
+    (in memory from `sink`, when given: see loads)."""
+    data = _b64decode(obj["data"], sink)
     if obj["type"] == "numpy":
         if isinstance(data, memoryview) and not data.readonly:
             arr = _npy_view(data)
@@ -171,7 +176,7 @@ class _Encoder(json.JSONEncoder):
         return _encode(obj)
 
 
-def _decode(d: dict):
+def _decode(d: dict, sink=None):
     t = d.get("__type__")
     if t is None:
         return d
@@ -182,7 +187,7 @@ def _decode(d: dict):
     if t == "DeviceTensorPointer":
         return DeviceTensorPointer(d["inf_name"], getattr(_torch(), _dtype_name(d["dtype"])))
     if t == "HostTensor":
-        return HostTensor(decode_tensor(d["tensor_base64"]))
+        return HostTensor(decode_tensor(d["tensor_base64"], sink))
     if t == "DeviceOpArg":
         return DeviceOpArg(d["arg_type"], d["value"])
     if t == "DeviceOp":
@@ -241,9 +246,13 @@ def _lift(raw: bytes, tag: bytes):
     return b"".join(pieces), spans
 
 
-def loads(text) -> ExecutionTranscript:
+def loads(text, sink=None) -> ExecutionTranscript:
     """A transcript from its JSON text (str or UTF-8 bytes); the same object
-    HEAL's load_transcript_from_json makes of it (serialization.py:143-148)."""
+    HEAL's load_transcript_from_json makes of it (serialization.py:143-148).
+    With `sink`, every payload the C library decodes is written into
+    sink(nbytes), a writable 1-D uint8 array the caller provides (a server
+    passes pinned host memory, so that a numpy payload is ready for an
+    asynchronous upload where it lands)."""
     try:
         raw = text.encode("utf-8") if isinstance(text, str) else bytes(text)
     except UnicodeEncodeError:
@@ -266,7 +275,7 @@ def loads(text) -> ExecutionTranscript:
         if d.get("__type__") == "HostTensor" and isinstance(d.get("tensor_base64"), dict) and \
                 isinstance(d["tensor_base64"].get("data"), _Payload):
             count["used"] += 1
-        return _decode(d)
+        return _decode(d, sink)
 
     out = json.loads(skeleton, object_hook=hook)
     if count["cut"] != count["used"]:

@@ -42,7 +42,9 @@ completion (observed by polling the event) minus arrival.
 from __future__ import annotations
 
 import bisect
+import concurrent.futures as cf
 import ctypes
+import threading
 import time
 from dataclasses import dataclass, field
 
@@ -106,6 +108,7 @@ class Request:
 
     fused: bool = False
     host_diag: object = None  # decoded from the request's transcript (else the server's own matrix)
+    host_buf: object = None   # the pinned byte buffer host_diag lies in, when it was decoded in place
 
     def footprint(self) -> int:
         """Device bytes the request holds while in flight: the rotated stack
@@ -136,15 +139,16 @@ def matvec_transcript(ct: str, diagonals) -> str:
     [d, 1, 1, d, L] (int64; a numpy array travels as np.save bytes, a torch
     tensor as torch.save bytes, both base64, as HEAL encodes them),
     `matvec` of resident ciphertext `ct` by them, download of the result
-    [2, N, L].  The download's expected tensor is an empty placeholder: the
-    client has no result to verify."""
+    [2, N, L].  The download's expected tensor is an empty placeholder (in
+    the diagonals' own encoding): the client has no result to verify."""
     import torch
     from .runtime import DeviceTensorPointer, TranscriptBuilder, dumps
     tb = TranscriptBuilder(prefix="r")
     tb.segment("matvec")
     dg = tb.host_to_device(diagonals)
     out = tb.op("matvec", DeviceTensorPointer(ct, torch.int64), dg, int(diagonals.shape[0]), dtype=torch.int64)
-    tb.device_to_host(out, torch.zeros(0, dtype=torch.int64))
+    empty = np.zeros(0, np.int64) if isinstance(diagonals, np.ndarray) else torch.zeros(0, dtype=torch.int64)
+    tb.device_to_host(out, empty)
     tb.free(dg, out)
     tb.end_segment()
     return dumps(tb.transcript())
@@ -209,16 +213,20 @@ def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max
     TimeoutError, so a device that stopped answering ends the loop instead
     of leaving it polling.  With `intake`, each request is replaced on
     arrival by intake(request) (a transcript decoded into the request it
-    describes); the time it takes counts toward the request's latency."""
+    describes), or by a concurrent.futures.Future of it (decoded on another
+    thread): a request is admitted only once it is decoded, still in
+    arrival order, and a decoding error ends the loop with that error.
+    The decoding time counts toward the request's latency."""
     pending = sorted(requests, key=lambda r: r.arrival)
-    queue, inflight, st = [], [], LoopStats()
+    queue, inflight, st = [], [], LoopStats()   # queue: (index in pending, request or its Future)
     nxt, t0 = 0, clock()
     while nxt < len(pending) or queue or inflight:
         now = clock() - t0
         while nxt < len(pending) and pending[nxt].arrival <= now:
-            if intake is not None:
-                pending[nxt] = intake(pending[nxt])
-            queue.append(pending[nxt])
+            item = pending[nxt] if intake is None else intake(pending[nxt])
+            if not isinstance(item, cf.Future):
+                pending[nxt] = item
+            queue.append((nxt, item))
             nxt += 1
         st.max_queue = max(st.max_queue, len(queue))
         progressed = False
@@ -235,7 +243,12 @@ def serve(requests, arena: Arena, issue, clock=time.perf_counter, idle=None, max
                 raise TimeoutError(f"request {req.rid} unfinished {now - req.admitted:.3f} s after admission "
                                    f"(limit {timeout} s)")
         while queue and len(inflight) < max_inflight:
-            req = queue[0]
+            idx, req = queue[0]
+            if isinstance(req, cf.Future):
+                if not req.done():
+                    break
+                req = pending[idx] = req.result()
+                queue[0] = (idx, req)
             off = arena.alloc(req.footprint())
             if off is None:
                 if not inflight:
@@ -298,6 +311,8 @@ class MatVecServer:
         self.out_host = {}
         self.keep = set()                    # request ids whose output is kept
         self.pinned = {}                     # shape -> free pinned buffers for decoded diagonals
+        self.pinned_bytes = {}               # size -> free pinned byte buffers that payloads decode into
+        self.pool_lock = threading.Lock()    # the pools are shared with the intake threads
 
     # views into the arena
     def _view(self, off, shape):
@@ -369,11 +384,13 @@ class MatVecServer:
         return Handle()
 
     def recycle(self, req: Request):
-        """Returns a decoded request's pinned diagonals buffer to the pool
-        (once nothing reads it any more)."""
-        if req.host_diag is not None:
-            self.pinned.setdefault(tuple(req.host_diag.shape), []).append(req.host_diag)
-            req.host_diag = None
+        """Returns a decoded request's pinned buffer to its pool (once
+        nothing reads it any more)."""
+        if req.host_buf is not None:
+            self._give(self.pinned_bytes, req.host_buf.numel(), req.host_buf)
+        elif req.host_diag is not None:
+            self._give(self.pinned, tuple(req.host_diag.shape), req.host_diag)
+        req.host_diag = req.host_buf = None
 
     def split_ms(self, req: Request, reps: int = 5) -> dict:
         """Median CUDA-event time of each HEAL call of the request (its
@@ -400,26 +417,63 @@ class MatVecServer:
             self.capi.check(self.capi.lib().heal_set_stream(None))
             self.arena.free(off)
 
+    def _take(self, pool: dict, key, make):
+        with self.pool_lock:
+            free = pool.get(key)
+            if free:
+                return free.pop()
+        return make()
+
+    def _give(self, pool: dict, key, buf):
+        with self.pool_lock:
+            pool.setdefault(key, []).append(buf)
+
     def from_transcript(self, text, rid: int, arrival: float) -> Request:
         """Decodes a matvec request transcript (JSON text, or its UTF-8 bytes
-        as they arrive) into a Request on a resident ciphertext; the
-        diagonals are copied into a pinned buffer (from a pool; it returns
-        there when the request completes) for the request's asynchronous
-        upload.  The payload is decoded by the C library's base64 decoder
-        and, for a numpy payload, used in place (runtime.serialization)."""
+        as they arrive) into a Request on a resident ciphertext.  The
+        payload is decoded by the C library's base64 decoder straight into a
+        pinned byte buffer from a pool, and a numpy payload is uploaded from
+        where it lands; any other payload (torch.save bytes, Fortran order)
+        is copied into a pinned buffer first.  The buffers return to their
+        pools when the request completes.  Safe to call from several
+        threads at once."""
         from .runtime import loads
-        name, d, diag = parse_matvec_transcript(loads(text))
+        torch = self.torch
+        handed = []
+
+        def sink(nbytes):
+            buf = self._take(self.pinned_bytes, nbytes,
+                             lambda: torch.empty(nbytes, dtype=torch.uint8, pin_memory=True))
+            handed.append(buf)
+            return buf.numpy()
+
         try:
-            tag, n, l, c = name.split("/")
-            n, l, c = int(n), int(l), int(c)
-            assert tag == "ct" and (n, l) in self.ct and 0 <= c < len(self.ct[(n, l)])
-        except (ValueError, AssertionError):
-            raise ValueError(f"no resident ciphertext named {name!r}") from None
-        if d not in self.ds or n % d or tuple(diag.shape) != (d, 1, 1, d, l):
-            raise ValueError(f"request of d = {d} on {name} does not fit the server")
-        src = self.torch.as_tensor(diag, dtype=self.torch.int64)
-        pool = self.pinned.setdefault(tuple(src.shape), [])
-        host = pool.pop() if pool else self.torch.empty(tuple(src.shape), dtype=self.torch.int64, pin_memory=True)
+            name, d, diag = parse_matvec_transcript(loads(text, sink=sink))
+            try:
+                tag, n, l, c = name.split("/")
+                n, l, c = int(n), int(l), int(c)
+                assert tag == "ct" and (n, l) in self.ct and 0 <= c < len(self.ct[(n, l)])
+            except (ValueError, AssertionError):
+                raise ValueError(f"no resident ciphertext named {name!r}") from None
+            if d not in self.ds or n % d or tuple(diag.shape) != (d, 1, 1, d, l):
+                raise ValueError(f"request of d = {d} on {name} does not fit the server")
+        except BaseException:
+            for buf in handed:
+                self._give(self.pinned_bytes, buf.numel(), buf)
+            raise
+        owner = None
+        if isinstance(diag, np.ndarray) and diag.dtype == np.int64 and diag.flags.c_contiguous:
+            ptr = diag.ctypes.data
+            owner = next((b for b in handed if b.data_ptr() <= ptr and ptr + diag.nbytes <= b.data_ptr() + b.numel()),
+                         None)
+        for buf in handed:
+            if buf is not owner:
+                self._give(self.pinned_bytes, buf.numel(), buf)
+        if owner is not None:
+            return Request(rid, arrival, n, l, d, c, -1, host_diag=torch.from_numpy(diag), host_buf=owner)
+        src = torch.as_tensor(diag, dtype=torch.int64)
+        host = self._take(self.pinned, tuple(src.shape),
+                          lambda: torch.empty(tuple(src.shape), dtype=torch.int64, pin_memory=True))
         host.copy_(src)
         return Request(rid, arrival, n, l, d, c, -1, host_diag=host)
 
@@ -446,24 +500,34 @@ class MatVecServer:
                     self.alone(Request(rid, 0.0, n, l, d, 0, 0))
         self.torch.cuda.synchronize()
 
-    def run(self, requests, keep=(), timeout: float | None = 60.0, transcripts=None):
+    def run(self, requests, keep=(), timeout: float | None = 60.0, transcripts=None, intake_threads: int = 0):
         """Serves `requests`; a request still unfinished `timeout` seconds
         after its admission (admitted requests take milliseconds) raises
-        TimeoutError.  With `transcripts` ({rid: JSON text}), a request whose
-        rid has one arrives as that transcript and is decoded on arrival."""
+        TimeoutError.  With `transcripts` ({rid: JSON text or bytes}), a
+        request whose rid has one arrives as that transcript and is decoded
+        on arrival: on the loop's thread, or with `intake_threads` > 0 on
+        that many worker threads while the loop keeps admitting and
+        completing requests (the base64 decoding runs in the C library
+        without the interpreter lock)."""
         for r in requests:
             r.fused = self.fused
         self.keep = set(keep)
         self.out_host = {}
-        intake = None
-        if transcripts:
-            def intake(r):
-                if r.rid not in transcripts:
-                    return r
-                q = self.from_transcript(transcripts[r.rid], r.rid, r.arrival)
-                q.fused = self.fused
-                return q
-        return serve(requests, self.arena, self.issue, timeout=timeout, intake=intake)
+        if not transcripts:
+            return serve(requests, self.arena, self.issue, timeout=timeout)
+
+        def decode(r):
+            q = self.from_transcript(transcripts[r.rid], r.rid, r.arrival)
+            q.fused = self.fused
+            return q
+
+        if intake_threads <= 0:
+            return serve(requests, self.arena, self.issue, timeout=timeout,
+                         intake=lambda r: decode(r) if r.rid in transcripts else r)
+        with cf.ThreadPoolExecutor(max_workers=intake_threads) as pool:
+            # the polling loop yields the interpreter lock whenever it has nothing to do
+            return serve(requests, self.arena, self.issue, timeout=timeout, idle=lambda: time.sleep(0),
+                         intake=lambda r: pool.submit(decode, r) if r.rid in transcripts else r)
 
     @staticmethod
     def bytes_moved(req: Request) -> int:

@@ -74,9 +74,11 @@ def test_large_transcripts_decoded_natively():
         diag = srv.host_mats[(r.d, r.l, r.mat)][r.n]
         texts[r.rid] = S.matvec_transcript(S.ct_name(r.n, r.l, r.ct), diag.numpy() if r.rid % 2 else diag).encode()
     direct = {r.rid: srv.alone(S.Request(r.rid, 0.0, r.n, r.l, r.d, r.ct, r.mat)) for r in reqs}
-    st = srv.run(reqs, keep=[r.rid for r in reqs], transcripts=texts)
-    assert len(st.latencies) == len(reqs)
-    for r in reqs:
-        assert np.array_equal(srv.out_host[r.rid], direct[r.rid]), r
+    for threads in (0, 3):  # decoded on the loop's thread, then on three intake threads
+        st = srv.run(reqs, keep=[r.rid for r in reqs], transcripts=texts, intake_threads=threads)
+        assert len(st.latencies) == len(reqs)
+        for r in reqs:
+            assert np.array_equal(srv.out_host[r.rid], direct[r.rid]), (threads, r)
     for r in reqs[:4]:
         assert np.array_equal(srv.out_host[r.rid], oracle_product(srv, r)), r
+    assert srv.pinned_bytes  # numpy payloads landed in pooled pinned buffers

@@ -167,3 +167,45 @@ def test_intake_decodes_each_request_on_arrival():
     reqs = [S.Request(i, 0.0, 256, 2, 4, 0, 0) for i in range(5)]
     st = S.serve(reqs, S.Arena(1 << 20), lambda r, off: Done(), intake=intake)
     assert seen == list(range(5)) and len(st.latencies) == 5
+
+
+def test_intake_on_worker_threads_keeps_arrival_order():
+    """With an intake that returns Futures (decoding on worker threads, some
+    slower than others), requests are still admitted in arrival order, each
+    only once decoded, and every one completes; a decoding error ends the
+    loop with that error."""
+    import concurrent.futures as cf
+    import random
+    import time as _time
+
+    rng = random.Random(5)
+    delays = {i: rng.choice([0.0, 0.0005, 0.002]) for i in range(40)}
+    order = []
+
+    def decode(r):
+        _time.sleep(delays.get(r.rid, 0.0))
+        if r.rid == 999:
+            raise ValueError("no resident ciphertext named 'x'")
+        return S.Request(r.rid, r.arrival, r.n, r.l, r.d, r.ct, r.mat)
+
+    class Done:
+        def query(self):
+            return True
+
+        def finish(self):
+            pass
+
+    def issue(req, off):
+        order.append(req.rid)
+        return Done()
+
+    reqs = [S.Request(i, i * 1e-4, 256, 2, 4, 0, 0) for i in range(40)]
+    with cf.ThreadPoolExecutor(max_workers=4) as pool:
+        st = S.serve(reqs, S.Arena(1 << 24), issue, intake=lambda r: pool.submit(decode, r),
+                     idle=lambda: _time.sleep(0))
+    assert order == list(range(40)) and len(st.latencies) == 40
+    assert st.span > 0 and all(x > 0 for x in st.latencies)
+    bad = [S.Request(0, 0.0, 256, 2, 4, 0, 0), S.Request(999, 0.0, 256, 2, 4, 0, 0)]
+    with cf.ThreadPoolExecutor(max_workers=2) as pool:
+        with pytest.raises(ValueError, match="resident"):
+            S.serve(bad, S.Arena(1 << 24), issue, intake=lambda r: pool.submit(decode, r))
