@@ -300,19 +300,26 @@ def our_arm(args):
         if world > 1:
             torch.distributed.barrier()
 
-    # host time of the last timed loop's enqueueing (perf_counter around the
-    # loop): when it approaches the device time, the host bounds the rate
-    host_ms = {"last": 0.0}
+    # host time to enqueue the first HOST_SAMPLE chains of the last timed
+    # loop, while the device's launch queue still has room (later launches
+    # wait for queue space, so the loop as a whole advances at the device's
+    # pace): the host's own cost per chain, to compare with the device time
+    HOST_SAMPLE = 32
+    host_ms = {"last": 0.0, "n": 1}
+
+    def enqueue(fn, steps):
+        h0 = time.perf_counter()
+        for s in range(steps):
+            fn(s)
+            if s + 1 == min(HOST_SAMPLE, steps):
+                host_ms["last"], host_ms["n"] = (time.perf_counter() - h0) * 1e3, s + 1
 
     def timed(fn, steps):
         barrier()
         start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = capi.launches()
         start.record(stream)
-        h0 = time.perf_counter()
-        for s in range(steps):
-            fn(s)
-        host_ms["last"] = (time.perf_counter() - h0) * 1e3
+        enqueue(fn, steps)
         stop.record(stream)
         stop.synchronize()
         barrier()
@@ -356,10 +363,7 @@ def our_arm(args):
         start.record(stream)
         for sd in sides:
             sd.wait_event(start)
-        h0 = time.perf_counter()
-        for s in range(steps):
-            fn(s)
-        host_ms["last"] = (time.perf_counter() - h0) * 1e3
+        enqueue(fn, steps)
         for sd in sides:
             joined = torch.cuda.Event()
             joined.record(sd)
@@ -377,7 +381,7 @@ def our_arm(args):
     with Clocks(local) as clk:
         ms, launches = timed2(chain_step2, nch)
     clocks = clk.summary()
-    host_us = {"resident": host_ms["last"] * 1e3 / nch}
+    host_us = {"resident": host_ms["last"] * 1e3 / host_ms["n"]}
     value = whole_job_rate(nch, world, ms)
     for w in range(args.warmup):
         chain_step(w)
@@ -523,10 +527,7 @@ def our_arm(args):
         start.record(stream)
         s_in.wait_event(start)
         side.wait_event(start)
-        h0 = time.perf_counter()
-        for s in range(steps):
-            e2e_step(s)
-        host_ms["last"] = (time.perf_counter() - h0) * 1e3
+        enqueue(e2e_step, steps)
         for ev in ev_out:
             stream.wait_event(ev)
         stop.record(stream)
@@ -538,7 +539,7 @@ def our_arm(args):
         e2e_step(w)
     e2e_ms = e2e_timed(nch)
     e2e = whole_job_rate(nch, world, e2e_ms)
-    host_us["e2e"] = host_ms["last"] * 1e3 / nch
+    host_us["e2e"] = host_ms["last"] * 1e3 / host_ms["n"]
     torch.cuda.synchronize()
     want = outs[0].numpy()
     for p_ in pin_out:
