@@ -324,6 +324,7 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
   base.tw_s1 = tw->strides[1];
   base.q = mi.q;
   base.qone = mi.qone;
+  base.qone32 = mi.min_q > ((int64_t)1 << 32);  // then floor(2^64 / q) < 2^32 for every modulus
   base.bitrev = pi.bitrev_log;  // every table this call indexes is the bit reversal (its own inverse)
   base.diag = diag_device();
   if (inv) {

@@ -53,6 +53,7 @@ struct NttArgs {
   const uint64_t *qone;  // floor(2^64 / q) per limb: Shoup companion of 1 (growing-range reduction)
   int lazy_out;          // growing ranges, forward first pass: store unreduced values (below 2^63)
   int unreduced_in;      // the input is such a first pass's output (non-negative, possibly >= q)
+  int qone32;            // every modulus is above 2^32, so every qone fits in 32 bits
   const void *minv_pairs;
   const int *minv_neg;
   const void *minv_raw;
@@ -454,7 +455,8 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
         const int dist = 1 << (qn - 1 - kk);
 #pragma unroll
         for (int gl = 0; gl < (1 << kk); ++gl) {
-          const int64_t ti = (G << st) + ((int64_t)hi << kk) + gl;
+          // below 2m <= 2^25 (G < 2m / P, st < LOGP): 32-bit index arithmetic
+          const uint32_t ti = ((uint32_t)G << st) + ((uint32_t)hi << kk) + (uint32_t)gl;
           const Pair pr = TWS ? twp[ti] : __ldg(twp + ti);
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
@@ -552,6 +554,12 @@ __device__ __forceinline__ void reg_steps(typename Word<mode_wide(MODE)>::W (&v)
     reg_step<MODE, INV, LOGP, STEP, TWS, LPT>(v, r, G, twp, q);
     reg_steps<MODE, INV, LOGP, STEP + 1, TWS, LPT>(v, r, c, logC, tile, G, twp, q);
   }
+}
+
+// High 64 bits of a * b for b < 2^32: (a_hi b + floor(a_lo b / 2^32)) / 2^32,
+// the sum below 2^64 (the dropped low word of a_lo b cannot carry into it)
+__device__ __forceinline__ uint64_t mulhi64_u32(uint64_t a, uint32_t b) {
+  return ((uint64_t)(uint32_t)(a >> 32) * b + __umulhi((uint32_t)a, b)) >> 32;
 }
 
 // minimum resident 512-thread CTAs per SM the register allocation must allow
@@ -657,10 +665,18 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
   if (MODE == MODE_W64_GROW) {
     if (INV ? !g.scale : !g.lazy_out) {
       const W one = (W)g.qone[tq];
+      if (g.qone32) {  // floor(2^64 / q) below 2^32: a three-instruction high product
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) {
-        const W u = v[e] - (W)mulhi64((uint64_t)v[e], (uint64_t)one) * q;
-        v[e] = u >= q ? u - q : u;
+        for (int e = 0; e < kPT; ++e) {
+          const W u = v[e] - (W)mulhi64_u32((uint64_t)v[e], (uint32_t)one) * q;
+          v[e] = u >= q ? u - q : u;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < kPT; ++e) {
+          const W u = v[e] - (W)mulhi64((uint64_t)v[e], (uint64_t)one) * q;
+          v[e] = u >= q ? u - q : u;
+        }
       }
     }
   } else {

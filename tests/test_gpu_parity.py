@@ -552,3 +552,22 @@ def test_butterfly_peak_diagnostic():
     assert 1e10 < rate.value < 1e14              # butterflies per second on one GPU
     assert L.heal_ntt_butterfly_peak(0, ctypes.byref(rate)) == 1
     assert L.heal_ntt_butterfly_peak(16, None) == 1
+
+
+@pytest.mark.parametrize("m", [8192, 1 << 16])
+@pytest.mark.parametrize("bounds", [(2**32,), (2**32 + 2**26,), (2**32 + 2**26, 2**32)],
+                         ids=["below_2_32", "above_2_32", "mixed"])
+def test_growing_range_reduction_around_2_32(m, bounds):
+    """Each growing-range pass that reduces ends with a Shoup product by 1;
+    when every modulus is above 2^32 its companion floor(2^64 / q) fits in
+    32 bits and the high product is the short one.  Moduli just below 2^32
+    (the long product), just above (the short one), and both in one call
+    (the long one for all) against the oracle, both directions."""
+    qs = np.concatenate([np.asarray(P.ntt_primes(b, m, 2), np.int64) for b in bounds])
+    assert (qs > 2**31).all() and (qs < 2**33).all()
+    p, perm, tw, itw, minv = P.ntt_tables(qs, m)
+    a = P.residues(m + len(bounds), (2, m, 1, len(qs)), qs)
+    fw = ntt(a, p, perm, tw)
+    assert np.array_equal(fw, O.ntt(a, p, perm, tw))
+    assert np.array_equal(intt(fw, p, perm, itw, minv), a)
+    assert np.array_equal(intt(a, p, perm, itw, minv), O.intt(a, p, perm, itw, minv, exact=1))
