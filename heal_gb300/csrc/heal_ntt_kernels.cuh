@@ -595,12 +595,19 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
   // them all.
   const int64_t rowmul = g.kind == KIND_BLOCK ? 1 : g.nsets;
   int64_t raw[kPT];
-  int neg = 0;
+  // forward: one unsigned compare per point flags negative values and, with
+  // canon_load, values at or above q; inverse: the values that need the
+  // exact path
+  int big = 0;
+  auto flag = [&](int64_t w) {
+    if constexpr (INV) return needs_exact<INV>(g, w, q64);
+    return g.canon_load ? (uint64_t)w >= (uint64_t)q64 : w < 0;
+  };
   if (g.load_map && !g.bitrev) {
 #pragma unroll
     for (int e = 0; e < kPT; ++e) {
       raw[e] = act ? load_point<T>(g, x, point_of<INV, LOGP, kLPT>(0, r, e), t) : 0;
-      neg |= needs_exact<INV>(g, raw[e], q64);
+      big |= flag(raw[e]);
     }
   } else if (g.load_map) {
     // gather through the bit reversal: a thread's rows are row0 | d_e with
@@ -613,7 +620,7 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
     for (int e = 0; e < kPT; ++e) {
       const uint32_t de = (uint32_t)(point_of<INV, LOGP, kLPT>(0, 0, e) * rowmul);
       raw[e] = act ? (int64_t)p0[(int64_t)(rb | (__brev(de) >> sh)) * g.ss[1]] : 0;
-      neg |= needs_exact<INV>(g, raw[e], q64);
+      big |= flag(raw[e]);
     }
   } else {
     const int64_t ts = GDEC ? tq / g.gdec_power : tq;  // source limb
@@ -629,7 +636,16 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
         raw[e] = gdec_load<T>(g, raw[e], d, x.i, x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, e)), x.j, ts);
     }
 #pragma unroll
-    for (int e = 0; e < kPT; ++e) neg |= needs_exact<INV>(g, raw[e], q64);
+    for (int e = 0; e < kPT; ++e) big |= flag(raw[e]);
+  }
+  // The exact path takes a negative value, and for the inverse one at or
+  // above q as well (its first butterfly forms u + q - v); the forward
+  // reduces those on load instead.  The rare flagged threads tell them apart.
+  int neg = big;
+  if (!INV && g.canon_load && big) {
+    neg = 0;
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) neg |= raw[e] < 0;
   }
   const bool exact = __syncthreads_or(neg) || g.force_exact || (g.tw_neg && *g.tw_neg) ||
                      (g.scale && g.minv_neg && *g.minv_neg);
@@ -650,11 +666,23 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
   const W q = (W)q64;
   const Pair *twp = tw_row<Pair>(g, tq);
   W v[kPT];
+  if (INV) {
 #pragma unroll
-  for (int e = 0; e < kPT; ++e) {
-    uint64_t u = (uint64_t)raw[e];
-    if (g.canon_load && u >= (uint64_t)q64) u %= (uint64_t)q64;
-    v[e] = (W)u;
+    for (int e = 0; e < kPT; ++e) {
+      uint64_t u = (uint64_t)raw[e];
+      if (g.canon_load && u >= (uint64_t)q64) u %= (uint64_t)q64;
+      v[e] = (W)u;
+    }
+  } else if (big) {  // canonical load with values at or above q (none negative here)
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      uint64_t u = (uint64_t)raw[e];
+      if (u >= (uint64_t)q64) u %= (uint64_t)q64;
+      v[e] = (W)u;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) v[e] = (W)(uint64_t)raw[e];
   }
   reg_steps<MODE, INV, LOGP, 0>(v, r, c, logC, tile, x.G, twp, q);
 
