@@ -65,6 +65,8 @@ SIGNATURES = {
     "heal_host_alloc": ([_SZ, ctypes.POINTER(_VP)], ctypes.c_int),
     "heal_host_free": ([_VP], ctypes.c_int),
     "heal_base64_decode": ([_VP, _SZ, _VP, _SZ, ctypes.POINTER(_SZ), ctypes.c_int], ctypes.c_int),
+    "heal_set_reference_compat": ([ctypes.c_int], ctypes.c_int),
+    "heal_get_reference_compat": ([], ctypes.c_int),
     "heal_mark_modified": ([_VP], ctypes.c_int),
     "heal_copy_strided": ([_P, _P], ctypes.c_int),
     "heal_tensor_reshape": ([_P, _I32, ctypes.POINTER(_I64)], ctypes.c_int),

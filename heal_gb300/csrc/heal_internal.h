@@ -29,6 +29,8 @@ void clear_error();
 
 // ----------------------------------------------------------------- runtime
 int ensure_init();
+// heal_set_reference_compat: reproduce the sample implementation's wraparound
+bool reference_compat();
 cudaStream_t stream();
 bool capturing();  // a graph capture is open
 int device_sm_count();

@@ -335,7 +335,8 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
   }
   // m = 1 has no butterflies (the forward NTT is a plain copy, unreduced);
   // moduli >= 2^62 do not fit the 64-bit lazy ranges
-  base.force_exact = m == 1 || mi.max_q >= (int64_t(1) << 62);
+  base.literal = reference_compat();
+  base.force_exact = m == 1 || mi.max_q >= (int64_t(1) << 62) || base.literal;
   const bool is32 = dt == HEAL_INT32;
   NttPlan plan = plan_for(dt, inv, logm, k);
   if (t_collect && t_collect->force_first_log) {

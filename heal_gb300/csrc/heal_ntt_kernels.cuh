@@ -54,6 +54,7 @@ struct NttArgs {
   int lazy_out;          // growing ranges, forward first pass: store unreduced values (below 2^63)
   int unreduced_in;      // the input is such a first pass's output (non-negative, possibly >= q)
   int qone32;            // every modulus is above 2^32, so every qone fits in 32 bits
+  int literal;           // reference compatibility: sums and the m^-1 product wrap in the element type
   const void *minv_pairs;
   const int *minv_neg;
   const void *minv_raw;
@@ -255,6 +256,13 @@ __device__ __forceinline__ bool needs_exact(const NttArgs &g, int64_t x, int64_t
 }
 
 // ---------------------------------------------------------- exact path
+// x in the element type T with two's-complement wraparound (what the sample
+// implementation's int32 / int64 expressions compute), widened again
+template <typename T>
+__device__ __forceinline__ i128 wrap_elem(i128 x) {
+  return sizeof(T) == 4 ? (i128)(int32_t)(uint32_t)(uint64_t)x : (i128)(int64_t)(uint64_t)x;
+}
+
 // The tile (raw values, tidx layout) through the reference's arithmetic,
 // one stage per barrier; then stored (with m_inv scaling / gather).  TT is
 // the tile's word: int64, or the element type itself for int32 tensors
@@ -293,7 +301,16 @@ __device__ __noinline__ void exact_tile(const NttArgs &g, uint32_t block, TT *ti
       const int64_t u = tile[tidx(su, c, logC)];
       const int64_t v = tile[tidx(sv, c, logC)];
       int64_t nu, nv;
-      if (!INV) {
+      if (g.literal) {  // the sample implementation's sums in the element type (ntt_impl.cpp:106-107,155-157)
+        if (!INV) {
+          const int64_t vm = crem128((i128)v * s, q);
+          nu = crem128(wrap_elem<T>((i128)u + vm), q);
+          nv = crem128(wrap_elem<T>((i128)u + q - vm), q);
+        } else {
+          nu = crem128(wrap_elem<T>((i128)u + v), q);
+          nv = crem128(wrap_elem<T>((i128)u + q - v) * s, q);
+        }
+      } else if (!INV) {
         const int64_t vm = crem128((i128)v * s, q);
         nu = crem128((i128)u + vm, q);
         nv = crem128((i128)u + q - vm, q);
@@ -312,7 +329,11 @@ __device__ __noinline__ void exact_tile(const NttArgs &g, uint32_t block, TT *ti
     if (t >= g.k) continue;
     int64_t val = g.store_gather ? (int64_t)tile[tidx((int)perm_row(g, g.store_gather, s), c, logC)]
                                  : (int64_t)tile[tidx(s, c, logC)];
-    if (g.scale) val = crem128((i128)val * raw_any(g.minv_raw, t * g.minv_s0, is32), g.q[t]);
+    if (g.scale) {
+      const i128 prod = (i128)val * raw_any(g.minv_raw, t * g.minv_s0, is32);
+      // the sample implementation scales in the element type (ntt_impl.cpp:165)
+      val = crem128(g.literal ? wrap_elem<T>(prod) : prod, g.q[t]);
+    }
     store_point<T>(g, x, s, t, val);
   }
 }

@@ -52,6 +52,7 @@ struct AxisArgs {
   int64_t n;
   Diag *diag;
   int fast;                       // n and every dim below 2^32: 32-bit index math
+  int literal;                    // reference compatibility: the running sum wraps in the element type
   FastDiv fd[HEAL_MAX_DIMS];      // division by each result dim
 };
 
@@ -98,7 +99,10 @@ __global__ void __launch_bounds__(256) axis_modsum_kernel(const __grid_constant_
     constexpr int kBatch = 4;
     int64_t sum = 0;
     auto step = [&](int64_t v) {
-      if (sum >= 0 && v >= 0 && q > 0) {
+      if (g.literal) {  // (sum + a_r) in the element type, then % (axis_modsum_impl.cpp:70)
+        const i128 x = (i128)sum + (i128)v;
+        sum = crem128(sizeof(T) == 4 ? (i128)(int32_t)(uint32_t)(uint64_t)x : (i128)(int64_t)(uint64_t)x, q);
+      } else if (sum >= 0 && v >= 0 && q > 0) {
         uint64_t x = (uint64_t)sum + (uint64_t)v;
         sum = v < q ? (int64_t)(x >= (uint64_t)q ? x - (uint64_t)q : x) : (int64_t)(x % (uint64_t)q);
       } else {
@@ -231,6 +235,7 @@ static int axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_te
     g.n = n;
     g.diag = diag_device();
     g.fast = n < (int64_t)UINT32_MAX;
+    g.literal = reference_compat();
     for (int i = 0; i < r->ndim; ++i) {
       if (r->dims[i] >= (int64_t)UINT32_MAX) g.fast = 0;
       else g.fd[i] = fastdiv_make((uint32_t)std::max<int64_t>(r->dims[i], 1));
@@ -239,7 +244,8 @@ static int axis_modsum(const heal_tensor *a, const heal_tensor *p, const heal_te
     // axes D times the strides of a dense row-major result, 16-byte aligned
     const int es = elem_size(r->dtype), vec = 16 / es;
     const int64_t D = g.ax_len;
-    bool blocks = g.ax_stride == 1 && D >= 2 && D <= 4 && r->ndim > 0 && dense_rowmajor(*r) && n % vec == 0 &&
+    bool blocks = !g.literal && g.ax_stride == 1 && D >= 2 && D <= 4 && r->ndim > 0 && dense_rowmajor(*r) &&
+                  n % vec == 0 &&
                   n < (int64_t)UINT32_MAX && (uintptr_t)A.data % 16 == 0 && (uintptr_t)r->data % 16 == 0;
     for (int i = 0; i < r->ndim && blocks; ++i) blocks = r->dims[i] == 1 || g.ai.strides[i] == D * r->strides[i];
     if (blocks) {

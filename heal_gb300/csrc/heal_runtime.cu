@@ -92,6 +92,10 @@ int ensure_init() {
 }
 
 cudaStream_t stream() { return g_rt.cur; }
+
+// the sample implementation's wraparound instead of exact results (heal_set_reference_compat)
+std::atomic<bool> g_reference_compat{false};
+bool reference_compat() { return g_reference_compat.load(); }
 int device_sm_count() { return g_rt.sms; }
 void note_launch(int n) { g_rt.launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 Diag *diag_device() { return g_rt.diag; }
@@ -1008,6 +1012,13 @@ int heal_set_stream(void *s) {
 }
 
 uint64_t heal_kernel_launch_count(void) { return g_rt.launches.load(); }
+
+int heal_set_reference_compat(int on) {
+  g_reference_compat.store(on != 0);
+  return HEAL_OK;
+}
+
+int heal_get_reference_compat(void) { return g_reference_compat.load() ? 1 : 0; }
 
 int heal_alloc(size_t bytes, int zero, void **out) {
   if (!out) return set_error(HEAL_ERR_INVALID_ARGUMENT, "heal_alloc: out must not be null");

@@ -92,6 +92,24 @@ int heal_set_stream(void *stream);
  * replay counts the kernels it contains). */
 uint64_t heal_kernel_launch_count(void);
 
+/* Reference-compatibility mode (off by default).  HEAL's sample
+ * implementation computes some sums and the INTT's m^-1 scaling in the
+ * element type, so they wrap: the int64 INTT for every modulus above about
+ * 2^31.5 (ntt_impl.cpp:165), the int32 NTT and INTT butterflies for moduli
+ * of 2^30 and above (ntt_impl.cpp:106-107,155-157), the int32 INTT scaling
+ * above about 2^15.5, and axis_modsum's running sum for int32 moduli of 2^30
+ * and int64 moduli of 2^62 and above (axis_modsum_impl.cpp:70).  This
+ * backend computes the mathematically exact results by default.  With
+ * on != 0, heal_ntt, heal_intt and heal_axis_modsum reproduce the sample
+ * implementation's wraparound instead (every NTT tile then takes the
+ * stage-by-stage exact path, so transforms are much slower), so that outputs
+ * equal the sample implementation's bit for bit even where it overflows.
+ * The extension ops (modmul_axis_sum, g_decomposition_ntt,
+ * modmul_axis_sum_permute, the batches) keep the exact semantics.  A process-
+ * wide setting; calls already enqueued are not affected. */
+int heal_set_reference_compat(int on);
+int heal_get_reference_compat(void);
+
 /* CUDA graphs of HEAL calls.  heal_graph_begin starts capturing the library
  * stream; every compute call until heal_graph_end is recorded instead of run,
  * and heal_graph_end returns an instantiated graph that heal_graph_launch
