@@ -375,19 +375,26 @@ static uint64_t g_cache_clock = 0;
 // keep every shape of a few hundred ciphertexts resident for graph capture.
 constexpr size_t kCacheMax = 4096;
 
+// Cache key: the kind, then per tensor its data pointer, dtype, ndim and
+// dims / strides as raw bytes (fixed widths, ndim before the dims, so no two
+// different argument lists give the same key), then `extra`.  Built on every
+// call that uses a derived table, so without any formatting.
 static std::string key_of(const char *kind, std::initializer_list<const heal_tensor *> ts, int64_t extra = 0) {
   std::string k(kind);
-  char buf[64];
+  k.reserve(k.size() + 16 + ts.size() * (24 + 16 * HEAL_MAX_DIMS));
+  auto put = [&k](const void *p, size_t n) { k.append((const char *)p, n); };
   for (const heal_tensor *t : ts) {
-    snprintf(buf, sizeof buf, "|%p:%d:%d", t->data, t->dtype, t->ndim);
-    k += buf;
-    for (int i = 0; i < t->ndim; ++i) {
-      snprintf(buf, sizeof buf, ",%lld/%lld", (long long)t->dims[i], (long long)t->strides[i]);
-      k += buf;
-    }
+    k.push_back('|');
+    put(&t->data, sizeof t->data);
+    put(&t->dtype, sizeof t->dtype);
+    put(&t->ndim, sizeof t->ndim);
+    const int nd = std::max(0, std::min<int>(t->ndim, HEAL_MAX_DIMS));
+    put(t->dims, nd * sizeof(int64_t));
+    put(t->strides, nd * sizeof(int64_t));
   }
-  snprintf(buf, sizeof buf, "#%lld", (long long)extra);
-  return k + buf;
+  k.push_back('#');
+  put(&extra, sizeof extra);
+  return k;
 }
 
 static void drop_entry(CacheEntry &e) {
