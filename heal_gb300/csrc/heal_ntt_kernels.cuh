@@ -583,6 +583,24 @@ __device__ __forceinline__ uint64_t mulhi64_u32(uint64_t a, uint32_t b) {
   return ((uint64_t)(uint32_t)(a >> 32) * b + __umulhi((uint32_t)a, b)) >> 32;
 }
 
+// The kPT addresses base + point_of(step, 0, e) * stride: point_of is a sum
+// of per-bit weights of e (a thread's points differ in disjoint bits), so
+// each address is an earlier one plus one weight * stride (kLPT products in
+// all, the rest additions), not a product per point.
+template <bool INV, int LOGP, int kLPT, int STEP, typename P>
+__device__ __forceinline__ void step_addresses(P *base, int64_t stride, P *(&out)[1 << kLPT]) {
+  int64_t w[kLPT];
+#pragma unroll
+  for (int i = 0; i < kLPT; ++i) w[i] = point_of<INV, LOGP, kLPT>(STEP, 0, 1 << i) * stride;
+  out[0] = base;
+#pragma unroll
+  for (int e = 1; e < (1 << kLPT); ++e) {
+    int low = 0;  // the lowest set bit of e (a constant after unrolling)
+    while (!((e >> low) & 1)) ++low;
+    out[e] = out[e & (e - 1)] + w[low];
+  }
+}
+
 // minimum resident 512-thread CTAs per SM the register allocation must allow
 // (2, at most 64 registers, measured fastest: 1 lets some kernels take more
 // registers and fewer warps, 3 caps at 40 registers and spills)
@@ -648,8 +666,15 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
     const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + ts * g.ss[3]) +
                   x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, 0)) * g.ss[1];
     const int64_t rs = rowmul * g.ss[1];
+    if constexpr (!INV && !GDEC) {  // (the inverse and g_decomposition kernels spill with it)
+      const T *pe[kPT];
+      step_addresses<INV, LOGP, kLPT, 0>(p0, rs, pe);
 #pragma unroll
-    for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)p0[point_of<INV, LOGP, kLPT>(0, 0, e) * rs] : 0;
+      for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)*pe[e] : 0;
+    } else {
+#pragma unroll
+      for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)p0[point_of<INV, LOGP, kLPT>(0, 0, e) * rs] : 0;
+    }
     if (GDEC && act) {
       const int d = (int)(tq - ts * g.gdec_power);
 #pragma unroll
@@ -781,11 +806,18 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
   T *p1 = (T *)g.dst + (x.i * g.ds[0] + x.j * g.ds[2] + t * g.ds[3]) +
           x.row_of(g, point_of<INV, LOGP, kLPT>(NSTEP - 1, r, 0)) * g.ds[1];
   const int64_t rsd = rowmul * g.ds[1];
+  if constexpr (!INV && !GDEC) {
+    T *pe[kPT];
+    step_addresses<INV, LOGP, kLPT, NSTEP - 1>(p1, rsd, pe);
 #pragma unroll
-  for (int e = 0; e < kPT; ++e) {
-    W val = v[e];
-    if (g.scale) val = mulw<WIDE>(val, mp, q);
-    p1[point_of<INV, LOGP, kLPT>(NSTEP - 1, 0, e) * rsd] = (T)(int64_t)val;
+    for (int e = 0; e < kPT; ++e) *pe[e] = (T)(int64_t)v[e];  // the forward has no m^-1 product
+  } else {
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      W val = v[e];
+      if (g.scale) val = mulw<WIDE>(val, mp, q);
+      p1[point_of<INV, LOGP, kLPT>(NSTEP - 1, 0, e) * rsd] = (T)(int64_t)val;
+    }
   }
 }
 
