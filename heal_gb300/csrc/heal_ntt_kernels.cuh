@@ -666,7 +666,7 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
     const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + ts * g.ss[3]) +
                   x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, 0)) * g.ss[1];
     const int64_t rs = rowmul * g.ss[1];
-    if constexpr (!INV && !GDEC) {  // (the inverse and g_decomposition kernels spill with it)
+    if constexpr (!INV) {  // (the inverse kernel spills with it)
       const T *pe[kPT];
       step_addresses<INV, LOGP, kLPT, 0>(p0, rs, pe);
 #pragma unroll
