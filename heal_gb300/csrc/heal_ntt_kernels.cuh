@@ -666,15 +666,10 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
     const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + ts * g.ss[3]) +
                   x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, 0)) * g.ss[1];
     const int64_t rs = rowmul * g.ss[1];
-    if constexpr (!INV) {  // (the inverse kernel spills with it)
-      const T *pe[kPT];
-      step_addresses<INV, LOGP, kLPT, 0>(p0, rs, pe);
+    const T *pe[kPT];
+    step_addresses<INV, LOGP, kLPT, 0>(p0, rs, pe);
 #pragma unroll
-      for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)*pe[e] : 0;
-    } else {
-#pragma unroll
-      for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)p0[point_of<INV, LOGP, kLPT>(0, 0, e) * rs] : 0;
-    }
+    for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)*pe[e] : 0;
     if (GDEC && act) {
       const int d = (int)(tq - ts * g.gdec_power);
 #pragma unroll
