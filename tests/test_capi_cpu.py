@@ -146,3 +146,15 @@ def test_header_is_plain_c(tmp_path):
                     f"-Wl,-rpath,{lib_dir}"], check=True)
     run = subprocess.run([str(tmp_path / "use_header")], capture_output=True, text=True, check=True)
     assert int(run.stdout) == len(names)
+
+
+def test_reference_compat_switch_is_host_state():
+    """heal_set_reference_compat only sets a process-wide flag (no GPU
+    call): off by default, on and off again as asked."""
+    L = capi.lib()
+    assert L.heal_get_reference_compat() == 0
+    try:
+        assert L.heal_set_reference_compat(7) == 0 and L.heal_get_reference_compat() == 1
+    finally:
+        assert L.heal_set_reference_compat(0) == 0
+    assert L.heal_get_reference_compat() == 0
