@@ -72,6 +72,7 @@ LITERAL_CASES = [
     ((2, 4096, 1, 3), np.int64, 2**50),
     ((1, 8192, 1, 2), np.int64, 2**50),
     ((2, 256, 1, 2), np.int64, 2**63),
+    ((1, 1 << 16, 1, 2), np.int32, 2**31),   # two 256-point passes: the staged int32 kernel's exact path
 ]
 
 
@@ -101,3 +102,21 @@ def test_axis_modsum_running_sum_wraps_like_the_reference(compat, dt, bound):
         want = O.axis_modsum(a, qs, axis, exact=False)
         assert not np.array_equal(want, O.axis_modsum(a, qs, axis, exact=True))
         assert np.array_equal(run("heal_axis_modsum", a, qs, axis, out_shape=shape, dtype=dt), want)
+
+
+def test_keyswitch_batch_equals_the_calls_in_compat_mode(compat):
+    """The persistent keyswitch batch takes the same literal arithmetic as the
+    calls it replaces (its INTT stage scales in the element type too)."""
+    from heal_gb300.configs import RaggedKeyswitch
+    rk = RaggedKeyswitch(count=4, logns=(12, 13), lmin=2, lmax=4, seed=17)
+    want = []
+    for i in range(len(rk.specs)):
+        rk.run_calls(i)
+        want.append(rk.outs[i].numpy())
+    for o in rk.outs:
+        capi.call("heal_copy_strided", capi.DeviceArray.from_numpy(np.zeros(o.shape, np.int64)), o)
+    rk.run_batched()
+    for i, w in enumerate(want):
+        assert np.array_equal(rk.outs[i].numpy(), w), i
+    # on these 50-bit moduli the literal INTT leaves negative residues in x
+    assert any((j["x"].numpy() < 0).any() for j in rk.jobs)
