@@ -131,7 +131,9 @@ for case, dt, shape, bound, seed in [("ntt_i64", np.int64, (2, 64, 3, 3), 2**40,
                                     ("ntt_i64_m1", np.int64, (2, 1, 2, 3), 2**40, 12),
                                     ("ntt_i64_m2", np.int64, (3, 2, 1, 2), 2**40, 13),
                                     ("ntt_i64_m4096", np.int64, (1, 4096, 1, 2), 2**40, 19),
-                                    ("ntt_i32", np.int32, (3, 32, 1, 2), 2**14, 14)]:
+                                    ("ntt_i32", np.int32, (3, 32, 1, 2), 2**14, 14),
+                                    # 31-bit moduli: the reference's int32 sums wrap (ntt_impl.cpp:106-107)
+                                    ("ntt_i32_q31", np.int32, (2, 64, 1, 3), 2**31, 15)]:
     n = shape[1]
     qs = P.ntt_primes(bound, max(n, 2), shape[3])
     p, perm, tw, itw, minv = P.ntt_tables(qs, n, dt)
@@ -221,6 +223,14 @@ for dt in (np.int32, np.int64):
     perms_b = np.stack([np.argsort(P.splitmix64(60 + i, 5)) for i in range(2)]).astype(dt)
     put(f"permute_{tag}", a=x, perms_a=perms_a, perms_b=perms_b,
         r12=ref_permute(x, perms_a, 1, 2), r03=ref_permute(x, perms_b, 0, 3))
+
+# ---- 6. axis_modsum's running sum wrapping in the element type (axis_modsum_impl.cpp:70): canonical
+#         residues of moduli near 2^31 (int32) and 2^63 (int64)
+for dt, bound in ((np.int32, 2**31), (np.int64, 2**63)):
+    tag = SUF[np.dtype(dt)]
+    qs = np.asarray(P.ntt_primes(bound, 8, 3), dt)
+    x = P.residues(61, (6, 40, 3), qs, dt)
+    put(f"axis_modsum_wrap_{tag}", a=x, p=qs, ax0=ref_axis_modsum(x, qs, 0), ax1=ref_axis_modsum(x, qs, 1))
 
 np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **small)
 

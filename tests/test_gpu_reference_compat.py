@@ -34,8 +34,8 @@ def compat():
         capi.check(lib.heal_set_reference_compat(0))
 
 
-@pytest.mark.parametrize("case", ["ntt_i64", "ntt_i64_m1", "ntt_i64_m2", "ntt_i64_m4096", "ntt_i32", "ntt_neg",
-                                  "ntt_pin"])
+@pytest.mark.parametrize("case", ["ntt_i64", "ntt_i64_m1", "ntt_i64_m2", "ntt_i64_m4096", "ntt_i32", "ntt_i32_q31",
+                                  "ntt_neg", "ntt_pin"])
 def test_golden_transforms_equal_the_reference_outputs(golden, compat, case):
     """Every golden transform, the INTTs whose 40-bit scaling overflows in
     the reference included (the exact mode skips those)."""
@@ -47,6 +47,14 @@ def test_golden_transforms_equal_the_reference_outputs(golden, compat, case):
     assert np.array_equal(intt(src, g["p"], g["perm"], g["itw"], g["minv"]), g["intt"])
     if "intt_a" in g:
         assert np.array_equal(intt(g["a"], g["p"], g["perm"], g["itw"], g["minv"]), g["intt_a"])
+
+
+@pytest.mark.parametrize("tag,dt", [("32", np.int32), ("64", np.int64)])
+def test_golden_axis_modsum_wrap_equals_the_reference(golden, compat, tag, dt):
+    g = golden(f"axis_modsum_wrap_{tag}")
+    for ax in (0, 1):
+        shape = tuple(d for i, d in enumerate(g["a"].shape) if i != ax)
+        assert np.array_equal(run("heal_axis_modsum", g["a"], g["p"], ax, out_shape=shape, dtype=dt), g[f"ax{ax}"])
 
 
 def test_keyswitch_intt_overflow_equals_the_reference(golden, compat):

@@ -277,3 +277,22 @@ def test_exact_axis_modsum_in_python_integers(dt, bits):
             for r in range(5):
                 s = trunc_mod(s + int(a[r, i, t]), q)
             assert int(got[i, t]) == s, (i, t)
+
+
+def test_wraparound_cases_pin_the_literal_mode(golden):
+    """The reference's own outputs where its element-type sums wrap: the int32
+    NTT / INTT at 31-bit moduli (ntt_impl.cpp:106-107,155-157,165) and
+    axis_modsum's running sum at moduli near 2^31 and 2^63
+    (axis_modsum_impl.cpp:70).  The literal mode reproduces them; the exact
+    mode does not."""
+    g = golden("ntt_i32_q31")
+    args = (g["p"], g["perm"], g["itw"], g["minv"])
+    assert np.array_equal(O.ntt(g["a"], g["p"], g["perm"], g["tw"], exact=False), g["ntt"])
+    assert np.array_equal(O.intt(g["ntt"], *args, exact=False), g["intt"])
+    assert np.array_equal(O.intt(g["a"], *args, exact=False), g["intt_a"])
+    assert not np.array_equal(O.ntt(g["a"], g["p"], g["perm"], g["tw"], exact=True), g["ntt"])
+    for tag in ("32", "64"):
+        g = golden(f"axis_modsum_wrap_{tag}")
+        for ax in (0, 1):
+            assert np.array_equal(O.axis_modsum(g["a"], g["p"], ax, exact=False), g[f"ax{ax}"])
+            assert not np.array_equal(O.axis_modsum(g["a"], g["p"], ax, exact=True), g[f"ax{ax}"])
