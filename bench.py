@@ -1099,7 +1099,9 @@ def ntt_probe(args):
     50-bit primes tiled 3x (the digit tensor of batch/2 chains); --probe int32:
     [batch, 65536, 1, 32] int32 under 31-bit primes (--probe int32-intt: its
     INTT); --probe ct-intt: the INTT
-    of [batch, 65536, 1, 24] int64 (the chain's ciphertext).  Prints one JSON
+    of [batch, 65536, 1, 24] int64 (the chain's ciphertext); --probe
+    gdec-digits: heal_g_decomposition_ntt of [batch, 65536, 1, 24] into the
+    [batch, 65536, 1, 72] digit transform (D = 3, base 2^17).  Prints one JSON
     line with the CUDA-event time per call."""
     import torch
     import heal_gb300
@@ -1122,11 +1124,15 @@ def ntt_probe(args):
         p, perm, tw, itw, minv = P.ntt_tables(qs, N)
         p_t, tw_t = np.repeat(p, D), np.repeat(tw, D, axis=0)
     shape = (args.batch, N, 1, k)
-    x = capi.DeviceArray.from_numpy(P.residues(3, shape, p_t, dt))
+    gdec = args.probe == "gdec-digits"
+    src_shape = (args.batch, N, 1, L) if gdec else shape
+    x = capi.DeviceArray.from_numpy(P.residues(3, src_shape, qs if gdec else p_t, dt))
     y = capi.DeviceArray.empty(shape, dt)
     dev = [capi.DeviceArray.from_numpy(v) for v in (p_t, perm, itw if inverse else tw_t, minv)]
     if inverse:
         call = lambda: capi.call("heal_intt", x, dev[0], dev[1], dev[2], dev[3], None, None, y)
+    elif gdec:
+        call = lambda: capi.call("heal_g_decomposition_ntt", x, D, BITS, dev[0], dev[1], dev[2], y)
     else:
         call = lambda: capi.call("heal_ntt", x, dev[0], dev[1], dev[2], None, None, y)
     for _ in range(args.warmup):
@@ -1141,9 +1147,10 @@ def ntt_probe(args):
     ms = start.elapsed_time(stop) / args.steps
     limbs = args.batch * k
     esz = np.dtype(dt).itemsize
+    nbytes = (src_shape[0] * src_shape[3] + limbs) * N * esz  # the source read once, the result written once
     print(json.dumps({"mode": "ntt", "probe": args.probe, "shape": list(shape), "ms_per_call": ms,
                       "limbs_per_s": limbs / (ms / 1e3),
-                      "algorithmic_GBps": 2 * limbs * N * esz / (ms / 1e3) / 1e9}), flush=True)
+                      "algorithmic_GBps": nbytes / (ms / 1e3) / 1e9}), flush=True)
     return 0
 
 
@@ -1253,7 +1260,7 @@ def main():
     ap.add_argument("--fused", action="store_true", help="--mode request: the fused path")
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--inflight", type=int, default=2, help="chains in flight on their own streams")
-    ap.add_argument("--probe", default="digits", choices=["digits", "int32", "int32-intt", "ct-intt"])
+    ap.add_argument("--probe", default="digits", choices=["digits", "int32", "int32-intt", "ct-intt", "gdec-digits"])
     args = ap.parse_args()
     unknown = set(args.configs.split(",")) - set(WORKLOADS) - {""}
     if unknown:
