@@ -291,11 +291,11 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
                                                    : MODE_W64_LAZY;
   const bool wide = mode == MODE_W64_LAZY;
   // 64-bit growing ranges where the headroom allows (heal_ntt_kernels.cuh):
-  // forward values stay below (1 + 2 log2 m) q <= 49q < 2^63; an inverse pass
-  // of P stages ends below 2^P q < 2^63
+  // forward values stay below (1 + 4 log2 m) q <= 97q < 2^63; an inverse pass
+  // of P stages ends below 2^(P+1) q < 2^63
   auto mode_of = [&](int pbits) {
     if (!wide) return mode;
-    const int lim = inv ? 63 - pbits : 57;
+    const int lim = inv ? 62 - pbits : 56;
     return mi.max_q < (int64_t(1) << lim) ? (int)MODE_W64_GROW : mode;
   };
   PermInfo pi;

@@ -93,21 +93,25 @@ struct Word<false> {
 //   0  32-bit words, values in [0, 2q)    (every q < 2^31)
 //   1  32-bit words, Harvey's lazy ranges (every q < 2^30: 4q < 2^32)
 //   2  64-bit words, Harvey's lazy ranges (every q < 2^62: 4q < 2^64)
-//   3  64-bit words, growing ranges       (q < 2^57 forward, q < 2^(63 - P) inverse)
+//   3  64-bit words, growing ranges       (q < 2^56 forward, q < 2^(62 - P) inverse)
 // Lazy butterflies keep forward values in [0, 4q) and inverse values in
 // [0, 2q) with one conditional subtraction per butterfly instead of three;
 // every pass still ends on canonical residues.
 // Growing ranges drop that subtraction too, using the headroom of 64-bit
-// words over the modulus.  Forward (Cooley-Tukey): with u < Bq and the Shoup
-// product t in [0, 2q), u + t and u - t + 2q both lie in [0, (B + 2)q), so a
-// canonical input is below (1 + 2s)q after s stages and below 49q after the
-// 24 stages of the longest transform.  A first pass hands its unreduced
+// words over the modulus.  Forward (Cooley-Tukey): the Shoup product t takes
+// its quotient from a three-multiply high product (mulhi64_3), up to 2 below
+// the exact one, so t lies in [0, 4q); with u < Bq, u + t and u - t + 4q both
+// lie in [0, (B + 4)q), so a canonical input is below (1 + 4s)q after s
+// stages and below 97q < 2^63 after the 24 stages of the longest transform
+// (q < 2^56).  A first pass hands its unreduced
 // values to the second (`lazy_out`); the last pass reduces once per point
 // with a Shoup product by 1 (companion floor(2^64 / q)).  Inverse
-// (Gentleman-Sande): the sum of two values below 2^s q is below 2^(s+1) q and
-// a - b + 2^s q is non-negative, so stage s adds the constant q << s; the
-// product goes back to [0, 2q); a pass of P stages ends below 2^P q and
-// reduces once per point (the m^-1 product does it on the last pass).
+// (Gentleman-Sande), with the same product in [0, 4q): values entering stage
+// s are below 2^(s+1) q (below q at s = 0), so a - b + 2^(s+1) q is
+// non-negative and stage s adds that constant; the sum stays below
+// 2^(s+2) q and the product below 4q <= 2^(s+2) q; a pass of P stages ends
+// below 2^(P+1) q and reduces once per point (the m^-1 product does it on the
+// last pass).
 enum { MODE_N32 = 0, MODE_N32_LAZY = 1, MODE_W64_LAZY = 2, MODE_W64_GROW = 3 };
 __host__ __device__ constexpr bool mode_wide(int mode) { return mode >= MODE_W64_LAZY; }
 
@@ -124,6 +128,22 @@ __host__ __device__ constexpr bool mode_wide(int mode) { return mode >= MODE_W64
 #endif
 __host__ __device__ constexpr int lpt_of(int mode, bool inv) {
   return (mode == MODE_N32 && !inv) ? HEAL_NTT_LPT_N32_FWD : HEAL_NTT_LPT;
+}
+
+// floor(a * b / 2^64) - e with e in {0, 1, 2}: of the four 32 x 32-bit
+// partial products, the low-by-low one is dropped and the two cross products
+// contribute only their high words.  The dropped parts sum to below 3 * 2^64,
+// hence the error.  Three multiplies instead of four, one of them 64-bit wide.
+__device__ __forceinline__ uint64_t mulhi64_3(uint64_t a, uint64_t b) {
+  const uint32_t al = (uint32_t)a, ah = (uint32_t)(a >> 32), bl = (uint32_t)b, bh = (uint32_t)(b >> 32);
+  return (uint64_t)ah * bh + __umulhi(ah, bl) + __umulhi(al, bh);
+}
+
+// The forward growing-range product: y * w mod q up to three extra q,
+// [0, 4q) for any y < 2^64 (Shoup with the quotient of mulhi64_3: the exact
+// quotient leaves [0, 2q), each missing unit of it one more q)
+__device__ __forceinline__ uint64_t mulw_grow(uint64_t y, ulonglong2 pr, uint64_t q) {
+  return y * pr.x - mulhi64_3(y, pr.y) * q;
 }
 
 // y * w mod q up to one extra q: [0, 2q) for any y (Shoup, no final step)
@@ -462,7 +482,7 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
   constexpr int P = 1 << LOGP;
   constexpr int st0 = kLPT * STEP;
   constexpr int qn = (LOGP - st0) < kLPT ? (LOGP - st0) : kLPT;
-  const W q2 = q + q;
+  const W q2 = q + q, q4 = q2 + q2;
 #pragma unroll
   for (int set = 0; set < (kPT >> qn); ++set) {
     const int id = (r << (kLPT - qn)) + set;
@@ -482,11 +502,11 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
 #pragma unroll
           for (int off = 0; off < dist; ++off) {
             const int a = base + gl * 2 * dist + off, b = a + dist;
-            if (GROW) {
+            if constexpr (GROW) {
               const W u = v[a];
-              const W tv = mulw_lazy<WIDE>(v[b], pr, q);
+              const W tv = (W)mulw_grow((uint64_t)v[b], pr, (uint64_t)q);
               v[a] = u + tv;
-              v[b] = u - tv + q2;
+              v[b] = u - tv + q4;
             } else if (LAZY) {
               W u = v[a];
               u = u >= q2 ? u - q2 : u;
@@ -505,7 +525,8 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
       } else {
         const int hi = id >> st0;
         const int dist = 1 << kk;
-        const W qs = q << st;  // growing ranges: every value entering stage st is below 2^st q
+        // growing ranges: every value entering stage st >= 1 is below 2^(st+1) q
+        const W qs = q << (st + 1);
         // one flat loop over the step's butterflies (group gl, offset off):
         // nested gl / off loops were left partly rolled at 16 points per
         // thread, which put v[] in local memory
@@ -519,10 +540,10 @@ __device__ __forceinline__ void reg_step(typename Word<mode_wide(MODE)>::W (&v)[
           }
           {
             const int a = base + gl * 2 * dist + off, b = a + dist;
-            if (GROW) {
+            if constexpr (GROW) {
               const W d = v[a] - v[b] + qs;
               v[a] = v[a] + v[b];
-              v[b] = mulw_lazy<WIDE>(d, pr, q);
+              v[b] = (W)mulw_grow((uint64_t)d, pr, (uint64_t)q);
             } else if (LAZY) {
               W s = v[a] + v[b];
               s = s >= q2 ? s - q2 : s;

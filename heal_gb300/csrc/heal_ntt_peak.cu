@@ -1,8 +1,8 @@
 // heal_ntt_peak.cu — the arithmetic ceiling of the NTT's 64-bit butterfly.
 //
 // heal_ntt_butterfly_peak times the forward growing-range butterfly of the
-// register kernel (heal_ntt_kernels.cuh: u + t, u - t + 2q with t the lazy
-// Shoup product) on operands that never leave registers: each thread holds 8
+// register kernel (heal_ntt_kernels.cuh: u + t, u - t + 4q with t the
+// growing-range Shoup product) on operands that never leave registers: each thread holds 8
 // words and the 7 twiddle pairs of one radix-8 group and runs `groups` groups
 // of 12 butterflies, with one load and one store per word.  The measured
 // rate is the integer-pipe roofline that an NTT pass, which also moves its
@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(128) butterfly_peak_kernel(uint64_t *data, con
   ulonglong2 t[7];
 #pragma unroll
   for (int e = 0; e < 7; ++e) t[e] = tw[(i + e) & 63];
-  const uint64_t q2 = q + q;
+  const uint64_t q4 = 4 * q;
   for (int it = 0; it < groups; ++it) {
 #pragma unroll
     for (int kk = 0; kk < 3; ++kk) {
@@ -37,9 +37,9 @@ __global__ void __launch_bounds__(128) butterfly_peak_kernel(uint64_t *data, con
         for (int off = 0; off < dist; ++off) {
           const int a = gl * 2 * dist + off, b = a + dist;
           const uint64_t u = v[a];
-          const uint64_t tv = mulw_lazy<true>(v[b], pr, q);
+          const uint64_t tv = mulw_grow(v[b], pr, q);
           v[a] = u + tv;
-          v[b] = u - tv + q2;
+          v[b] = u - tv + q4;
         }
       }
     }

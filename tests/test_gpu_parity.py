@@ -493,17 +493,20 @@ def test_permute_strided_sources_in_vector_units(dt):
 
 # ------------------------------------------- 64-bit growing-range boundaries
 # The 64-bit transforms skip per-butterfly reductions while the modulus leaves
-# headroom: forward for q < 2^57 (values stay below 49q), an inverse pass of P
-# stages for q < 2^(63 - P).  Primes just below and just above each threshold,
-# with pass splits that move the inverse's pass lengths across them.
+# headroom: forward for q < 2^56 (values stay below (1 + 4 log2 m) q), an
+# inverse pass of P stages for q < 2^(62 - P) (values below 2^(P+1) q).
+# Primes just below and just above each threshold, with pass splits that move
+# the inverse's pass lengths across them.
 GROW_CASES = [
     # (m, prime bound, first-pass log2 per call: 0 = one pass)
-    (1 << 16, 2**57, (8, 4, 12)),    # forward grows to 33q; inverse passes: lazy ranges
-    (1 << 16, 2**55, (8, 4, 12)),    # 8-stage inverse passes grow; 12-stage ones do not
-    (1 << 16, 2**51, (8, 4, 12)),    # every pass grows
-    (4096, 2**51, (0, 6)),           # one 12-stage pass at its inverse threshold
-    (4096, 2**52, (0, 6)),
-    (1 << 20, 2**57, (10, 8)),       # the forward's longest tested chain: 41q
+    (1 << 16, 2**57, (8, 4, 12)),    # above the forward's threshold: lazy ranges in both directions
+    (1 << 16, 2**56, (8, 4, 12)),    # forward grows to 65q < 2^62.1; inverse passes: lazy ranges
+    (1 << 16, 2**54, (8, 4, 12)),    # 8-stage inverse passes grow; 12-stage ones do not
+    (1 << 16, 2**55, (8, 4, 12)),    # 8-stage inverse passes just above their threshold
+    (1 << 16, 2**50, (8, 4, 12)),    # every pass grows
+    (4096, 2**50, (0, 6)),           # one 12-stage pass at its inverse threshold
+    (4096, 2**51, (0, 6)),
+    (1 << 20, 2**56, (10, 8)),       # the forward's longest tested chain: 81q < 2^62.4
 ]
 
 
