@@ -244,6 +244,8 @@ static int ntt_run(bool inv, const heal_tensor *a_in, const heal_tensor *p, cons
     bool ok = res->ndim == 4 && res->dims[3] == a_in->dims[3] * gd->power;
     for (int i = 0; ok && i < 3; ++i) ok = res->dims[i] == a_in->dims[i];
     if (!ok) return set_error(HEAL_ERR_INVALID_ARGUMENT, "Output must have shape [l, m, r, k * power].");
+    // the kernels split a digit limb into source limb and digit in 32 bits
+    if (res->dims[3] >= ((int64_t)1 << 31)) return set_error(HEAL_ERR_INVALID_ARGUMENT, "k * power must be below 2^31");
     Av = *a_in;
     Av.dims[3] = a_in->dims[3] * gd->power;
     a = &Av;

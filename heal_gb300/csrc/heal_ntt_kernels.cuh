@@ -244,6 +244,37 @@ __device__ __forceinline__ int64_t gdec_load(const NttArgs &g, int64_t value, in
   return (int64_t)gdec_digit<T>(value, (uint64_t)d, (uint64_t)g.gdec_bits, (1ull << g.gdec_bits) - 1);
 }
 
+// Digits d of a thread's loaded source values, in place, with the per-thread
+// shift, mask and residual shift formed once (the closed forms of gdec_digit
+// and gdec_residual).  Returns whether a d == 0 load failed the residual
+// check; the caller then records each such point (gdec_warn_points).
+template <typename T, int kPT>
+__device__ __forceinline__ bool gdec_digits(int64_t (&raw)[kPT], uint32_t d, const NttArgs &g) {
+  const uint64_t bits = (uint64_t)g.gdec_bits;  // below 64
+  const uint64_t mask = (1ull << bits) - 1;
+  bool bad = false;
+  if constexpr (sizeof(T) == 8) {
+    const uint64_t sh = (uint64_t)d * bits, rsh = (uint64_t)g.gdec_power * bits;
+    const uint32_t s = sh >= 64 ? 0u : (uint32_t)sh;
+    const uint64_t m = sh >= 64 ? 0ull : mask;  // digits past the word are 0
+    const bool check = d == 0 && rsh < 64;      // a residual shifted out entirely is 0
+    const uint32_t rs = check ? (uint32_t)rsh : 0u;
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      const uint64_t uv = (uint64_t)raw[e];
+      bad |= check && (int64_t)(uv >> rs) > 0;
+      raw[e] = (int64_t)((uv >> s) & m);
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < kPT; ++e) {
+      bad |= d == 0 && gdec_residual<T>(raw[e], (uint64_t)g.gdec_power, bits) > 0;
+      raw[e] = (int64_t)gdec_digit<T>(raw[e], (uint64_t)d, bits, mask);
+    }
+  }
+  return bad;
+}
+
 template <typename T, bool GDEC = false>
 __device__ __forceinline__ int64_t load_point(const NttArgs &g, const TileCtx &x, int s, int64_t t) {
   const int64_t v = x.row_of(g, s);
@@ -465,6 +496,25 @@ __device__ __forceinline__ int point_of(int step, int r, int e) {
   return (hi << (st0 + q)) + lo + (jj << st0);
 }
 
+// The rare path of gdec_digits, run after the tile's stores: reloads this
+// thread's source values and records every d == 0 load whose residual is
+// non-zero, with its coordinates, as the separate g_decomposition call does.
+// Out of line, with the tile recomputed from its index, so that the fast path
+// keeps no state for it.
+template <typename T, bool INV, int LOGP, int kLPT>
+__device__ __noinline__ void gdec_warn_points(const NttArgs &g, uint32_t block) {
+  const TileCtx x = tile_ctx(g, block);
+  const int r = threadIdx.x >> x.logC;
+  const int64_t t = x.t0 + (threadIdx.x & (x.C - 1));
+  if (t >= g.k) return;
+  const int64_t ts = t / g.gdec_power;
+  for (int e = 0; e < (1 << kLPT); ++e) {
+    const int64_t row = x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, e));
+    const int64_t v = (int64_t)((const T *)g.src)[x.i * g.ss[0] + row * g.ss[1] + x.j * g.ss[2] + ts * g.ss[3]];
+    if (gdec_residual<T>(v, (uint64_t)g.gdec_power, (uint64_t)g.gdec_bits) > 0) gdec_warn(g, x.i, row, x.j, ts);
+  }
+}
+
 // One register step: stages [kLPT*STEP, kLPT*STEP + qn) on the kPT >> qn
 // sets of 2^qn points this thread holds.  TWS: the twiddle row is in shared
 // memory (the staged kernel), else read through the read-only cache.  LPT:
@@ -632,7 +682,7 @@ __device__ __forceinline__ void step_addresses(P *base, int64_t stride, P *(&out
 // on load); a separate instantiation so that the plain kernels keep their
 // register allocation.
 template <typename T, int MODE, bool INV, int LOGP, bool GDEC>
-__device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
+__device__ __forceinline__ void ntt_reg_tile(const NttArgs &g, uint32_t block, bool &gdec_bad) {
   constexpr bool WIDE = mode_wide(MODE);
   constexpr bool LAZY = MODE != MODE_N32;
   constexpr int kLPT = lpt_of(MODE, INV), kPT = 1 << kLPT;
@@ -683,7 +733,8 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
       big |= flag(raw[e]);
     }
   } else {
-    const int64_t ts = GDEC ? tq / g.gdec_power : tq;  // source limb
+    // source limb (digit limbs below 2^31, checked on the host)
+    const int64_t ts = GDEC ? (int64_t)((uint32_t)tq / (uint32_t)g.gdec_power) : tq;
     const T *p0 = (const T *)g.src + (x.i * g.ss[0] + x.j * g.ss[2] + ts * g.ss[3]) +
                   x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, 0)) * g.ss[1];
     const int64_t rs = rowmul * g.ss[1];
@@ -692,10 +743,8 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
 #pragma unroll
     for (int e = 0; e < kPT; ++e) raw[e] = act ? (int64_t)*pe[e] : 0;
     if (GDEC && act) {
-      const int d = (int)(tq - ts * g.gdec_power);
-#pragma unroll
-      for (int e = 0; e < kPT; ++e)
-        raw[e] = gdec_load<T>(g, raw[e], d, x.i, x.row_of(g, point_of<INV, LOGP, kLPT>(0, r, e)), x.j, ts);
+      const uint32_t d = (uint32_t)tq - (uint32_t)ts * (uint32_t)g.gdec_power;
+      gdec_bad = gdec_digits<T>(raw, d, g);
     }
 #pragma unroll
     for (int e = 0; e < kPT; ++e) big |= flag(raw[e]);
@@ -835,6 +884,15 @@ __device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
       p1[point_of<INV, LOGP, kLPT>(NSTEP - 1, 0, e) * rsd] = (T)(int64_t)val;
     }
   }
+}
+
+// One tile of a pass; with GDEC, the capacity warnings of its digit loads
+// are recorded once its results are stored.
+template <typename T, int MODE, bool INV, int LOGP, bool GDEC>
+__device__ __forceinline__ void ntt_reg_body(const NttArgs &g, uint32_t block) {
+  bool gdec_bad = false;
+  ntt_reg_tile<T, MODE, INV, LOGP, GDEC>(g, block, gdec_bad);
+  if (GDEC && gdec_bad) gdec_warn_points<T, INV, LOGP, lpt_of(MODE, INV)>(g, block);
 }
 
 template <typename T, int MODE, bool INV, int LOGP, bool GDEC = false>
