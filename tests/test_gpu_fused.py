@@ -180,6 +180,7 @@ def random_perms(rng, rows, m, dt):
     (((7, 33, 4), (7, 33, 4)), 0, 1, 0),                 # gathered axis after the reduced one
     (((5, 9, 6, 4), (9, 1, 4)), 2, 0, 1),                # broadcast b, reduced axis after the gathered one
     (((3, 50, 2), (3, 50, 2)), 0, 1, 0),
+    (((2, 64, 1, 3, 6), (2, 64, 1, 3, 6)), 3, 2, 1),     # an even limb count
 ])
 def test_post_permute_matches_composition(dt, shapes, axis, ew, pa):
     rng = np.random.default_rng(31)
@@ -194,11 +195,12 @@ def test_post_permute_matches_composition(dt, shapes, axis, ew, pa):
 
 
 @pytest.mark.parametrize("dt", [np.int32, np.int64])
-def test_post_permute_non_canonical_and_duplicate_rows(dt):
+@pytest.mark.parametrize("k", [3, 4])
+def test_post_permute_non_canonical_and_duplicate_rows(dt, k):
     rng = np.random.default_rng(32)
-    p = np.array([97, 65521, 7], dtype=dt)
-    a = rng.integers(-1000, 100000, size=(2, 40, 1, 3, 3)).astype(dt)
-    b = rng.integers(-500, 3000, size=(2, 40, 1, 3, 3)).astype(dt)
+    p = np.array([97, 65521, 7, 40009][:k], dtype=dt)
+    a = rng.integers(-1000, 100000, size=(2, 40, 1, 3, k)).astype(dt)
+    b = rng.integers(-500, 3000, size=(2, 40, 1, 3, k)).astype(dt)
     perms = random_perms(rng, 1, 40, np.int32)
     perms[0, 7] = perms[0, 8]                          # two results read one row
     assert np.array_equal(fused_post(a, b, p, 3, perms, 2, 1), composed_post(a, b, p, 3, perms, 2, 1))
