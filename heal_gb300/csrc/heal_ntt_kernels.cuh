@@ -900,6 +900,20 @@ __global__ void __launch_bounds__(512, HEAL_NTT_MINB) ntt_reg_kernel(const __gri
   ntt_reg_body<T, MODE, INV, LOGP, GDEC>(g, blockIdx.x);
 }
 
+// The plain forward passes in 64-bit words at up to 72 registers: they do
+// not spill there, and at 7 resident CTAs of 128 threads per SM instead of 8
+// the digit NTT of the keyswitch measured 1.7-2.5% faster than at 64
+// registers.  The inverse passes and the first passes of
+// heal_g_decomposition_ntt measured best at 64 (1% slower at 72), and 80 was
+// slower for all.
+#ifndef HEAL_NTT_FWD64_REGS
+#define HEAL_NTT_FWD64_REGS 72
+#endif
+template <typename T, int MODE, bool INV, int LOGP, bool GDEC = false>
+__global__ void __maxnreg__(HEAL_NTT_FWD64_REGS) ntt_reg_kernel_fwd64(const __grid_constant__ NttArgs g) {
+  ntt_reg_body<T, MODE, INV, LOGP, GDEC>(g, blockIdx.x);
+}
+
 // ---------------------------------------------------------- ragged batch
 // One launch over the passes of up to kNttBatch transforms of one kernel
 // class (element type, arithmetic mode, direction, pass length, tile width):

@@ -76,6 +76,8 @@ static int launch_reg(const NttArgs &a, int64_t nblocks) {
   static bool attr = false;
   const int threads = ((1 << LOGP) >> lpt_of(MODE, INV)) * a.C;
   const size_t smem = (size_t)(1 << LOGP) * a.C * sizeof(int64_t);
+  if constexpr (!INV && !GDEC && mode_wide(MODE))
+    return launch_with_smem(ntt_reg_kernel_fwd64<T, MODE, INV, LOGP, GDEC>, a, nblocks, threads, smem, attr);
   return launch_with_smem(ntt_reg_kernel<T, MODE, INV, LOGP, GDEC>, a, nblocks, threads, smem, attr);
 }
 
