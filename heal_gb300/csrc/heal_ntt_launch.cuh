@@ -76,6 +76,9 @@ static int launch_reg(const NttArgs &a, int64_t nblocks) {
   static bool attr = false;
   const int threads = ((1 << LOGP) >> lpt_of(MODE, INV)) * a.C;
   const size_t smem = (size_t)(1 << LOGP) * a.C * sizeof(int64_t);
+  if constexpr (!INV && !GDEC && mode_wide(MODE) && LOGP == 8)
+    return launch_with_smem(ntt_reg_kernel_fwd64_r16<T, MODE, LOGP>, a, nblocks,
+                            ((1 << LOGP) >> kFwd64R16Lpt) * a.C, smem, attr);
   if constexpr (!INV && !GDEC && mode_wide(MODE))
     return launch_with_smem(ntt_reg_kernel_fwd64<T, MODE, INV, LOGP, GDEC>, a, nblocks, threads, smem, attr);
   return launch_with_smem(ntt_reg_kernel<T, MODE, INV, LOGP, GDEC>, a, nblocks, threads, smem, attr);

@@ -38,9 +38,10 @@ def tidx(s, c, logc):
 
 
 # (direction, log2 points per thread, shared word bytes) of the instantiated
-# register kernels: 64-bit words hold 8 points per thread; the forward
+# register kernels: 64-bit words hold 8 points per thread, and 16 in the
+# 256-point forward passes of the plain 64-bit transform; the forward
 # canonical 32-bit mode holds 16; the other 32-bit modes hold 8
-KINDS = [(False, 3, 8), (True, 3, 8), (False, 4, 4), (False, 3, 4), (True, 3, 4)]
+KINDS = [(False, 3, 8), (True, 3, 8), (False, 4, 8), (False, 4, 4), (False, 3, 4), (True, 3, 4)]
 SHAPES = [(inv, klpt, wb, logp, logc) for inv, klpt, wb in KINDS for logp in range(4, 13) for logc in range(5)
           if ((1 << logp) >> klpt) << logc <= 512]
 
