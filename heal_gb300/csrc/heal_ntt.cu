@@ -704,8 +704,9 @@ int heal_ntt_autotune(int inverse, const heal_tensor *a, const heal_tensor *p, c
   HEAL_TRY_CUDA(cudaEventCreate(&e0));
   HEAL_TRY_CUDA(cudaEventCreate(&e1));
   int rc = HEAL_OK;
-  float best_ms = 0.f;
-  NttPlan best = default_plan(logm);
+  float best_ms = 0.f, default_ms = 0.f;
+  const NttPlan dflt = default_plan(logm);
+  NttPlan best = dflt;
   for (const NttPlan &pl : cands) {
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
@@ -724,11 +725,16 @@ int heal_ntt_autotune(int inverse, const heal_tensor *a, const heal_tensor *p, c
     }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
+    if (pl.tile_limbs == dflt.tile_limbs && pl.first_log == dflt.first_log) default_ms = ms;
     if (best_ms == 0.f || ms < best_ms) {
       best_ms = ms;
       best = pl;
     }
   }
+  // plans within a few percent of each other swap places between runs: the
+  // default plan stays unless another is at least kTuneMargin faster
+  constexpr float kTuneMargin = 0.03f;
+  if (default_ms > 0.f && best_ms > default_ms * (1.f - kTuneMargin)) best = dflt;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   {

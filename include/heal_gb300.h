@@ -278,7 +278,8 @@ int heal_ntt_get_plan(int dtype, int inverse, int64_t m, int64_t k, int *tile_li
 int heal_ntt_clear_plans(void);
 /* Times every candidate plan on these operands (heal_ntt when inverse == 0,
  * else heal_intt with m_inv) with `reps` calls each and keeps the fastest for
- * this shape; `result` is overwritten.  The choice is returned through
+ * this shape, or the default plan unless the fastest beats it by 3% (near-equal
+ * plans swap places between runs); `result` is overwritten.  The choice is returned through
  * tile_limbs / first_pass_log2 (either may be null).  Waits for the GPU; fails
  * while a graph is being captured. */
 int heal_ntt_autotune(int inverse, const heal_tensor *a, const heal_tensor *p, const heal_tensor *perm,
